@@ -1,0 +1,178 @@
+/*
+ * hsr.h — C ABI of the GB300 draw path for Hana-SoftwareRenderer.
+ *
+ * The reference renders with one synchronous call,
+ *     void graphics_draw_triangle(DrawData* draw_data);          (graphics.h:15, graphics.cpp:378-407)
+ * where DrawData = {Model*, IShader*, RenderBuffer*}             (graphics.h:9-13)
+ * and the shader's ShaderData / Material carry the uniforms      (IShader.h:7-32).
+ *
+ * This header replaces that call with plain handles, pointers and sizes so that any
+ * host (C, C++, ctypes, cgo, JNI) can bind it.  Every entry point returns an int
+ * status (HSR_OK == 0).  No entry point falls back to the CPU: without a usable
+ * CUDA device hsr_init() fails and every other call returns HSR_ERR_NOT_INITIALIZED.
+ *
+ * Semantics kept from the reference (bit-exact unless noted):
+ *   - vertex() runs per face corner, clip / cull / viewport / bounding box / integer
+ *     pixel sampling / inclusive coverage exactly as graphics.cpp:7-376;
+ *   - the depth test is `skip if frag_depth > depth` (graphics.cpp:359): equal depth
+ *     passes and the later-submitted triangle wins;
+ *   - colour is written R,G,B only through (uchar)(c*255) truncation (renderbuffer.cpp:38-44);
+ *     alpha is never written by a draw;
+ *   - RGBA8 colour is within 1 LSB of the reference (powf is not correctly rounded).
+ *
+ * Buffers are row-major, index y*width + x, row 0 = bottom (maths.cpp:20-25).
+ */
+#ifndef HSR_H
+#define HSR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HSR_ABI_VERSION 1
+
+/* ---- status codes ---------------------------------------------------------------- */
+enum {
+  HSR_OK = 0,
+  HSR_ERR_INVALID_ARG = 1,     /* null pointer, bad size, index out of range            */
+  HSR_ERR_UNKNOWN_SHADER = 2,  /* shader kind outside hsr_shader_kind                   */
+  HSR_ERR_BIN_OVERFLOW = 3,    /* scratch capacity exceeded and retries exhausted       */
+  HSR_ERR_OUT_OF_MEMORY = 4,   /* device allocation failed / pool admission refused    */
+  HSR_ERR_TIMEOUT = 5,         /* a bounded device wait or host wait gave up            */
+  HSR_ERR_CUDA = 6,            /* CUDA runtime error (hsr_last_error() has the text)    */
+  HSR_ERR_NOT_INITIALIZED = 7, /* hsr_init() not called or failed                       */
+  HSR_ERR_BAD_HANDLE = 8,      /* unknown or released handle                            */
+  HSR_ERR_BUSY = 9             /* request not finished yet (hsr_poll / server polling)  */
+};
+
+/* ---- shader kinds: one per IShader subclass (IShader.h:132-165) -------------------- */
+typedef enum hsr_shader_kind {
+  HSR_SHADER_GROUND = 0,             /* GroundShader            IShader.cpp:5-15    */
+  HSR_SHADER_TOON = 1,               /* ToonShader              IShader.cpp:23-39   */
+  HSR_SHADER_TEXTURE = 2,            /* TextureShader           IShader.cpp:47-57   */
+  HSR_SHADER_TEXTURE_WITH_LIGHT = 3, /* TextureWithLightShader  IShader.cpp:65-77   */
+  HSR_SHADER_BLINN = 4,              /* BlinnShader             IShader.cpp:85-109  */
+  HSR_SHADER_NORMALMAP = 5,          /* NormalMapShader         IShader.cpp:117-162 */
+  HSR_SHADER_SHADOW = 6,             /* ShadowShader            IShader.cpp:170-180 */
+  HSR_SHADER_FLAT = 7,               /* test shader (no reference class): colour = bytes of
+                                        prim id (face + prim_base + 1), R low byte        */
+  HSR_SHADER_COUNT = 8
+} hsr_shader_kind;
+
+/* ---- uniforms: ShaderData (IShader.h:17-32) + Material scalars (IShader.h:7-15) ------
+ * Matrices are row-major, m[row*4 + col], the layout of Matrix4x4 rows (matrix.h:27).
+ * Colours are Color{r,g,b,a} (color.h).  The texture pointers of Material and the
+ * shadow_map RenderBuffer* travel as handles in hsr_draw_desc. */
+typedef struct hsr_shader_data {
+  float view_pos[3];          /* ShaderData::view_Pos   */
+  float light_dir[3];         /* ShaderData::light_dir  */
+  float light_color[4];       /* ShaderData::light_color */
+  float ambient[4];           /* ShaderData::ambient    */
+  float model_matrix[16];
+  float model_matrix_I[16];
+  float view_matrix[16];      /* carried for completeness; the draw path does not read it */
+  float projection_matrix[16];/* carried for completeness; the draw path does not read it */
+  float light_vp_matrix[16];
+  float camera_vp_matrix[16];
+  int32_t enable_shadow;      /* ShaderData::enable_shadow */
+  float material_color[4];    /* Material::color        */
+  float material_specular[4]; /* Material::specular     */
+  float gloss;                /* Material::gloss        */
+  float bump_scale;           /* Material::bump_scale   */
+} hsr_shader_data;
+
+typedef uint64_t hsr_mesh;     /* 0 is never a valid handle */
+typedef uint64_t hsr_texture;
+typedef uint64_t hsr_target;
+
+/* draw flags */
+#define HSR_DRAW_CLEAR 1u        /* clear the target to clear_rgba / clear_depth / prim 0
+                                    before drawing (fused: each pixel is written once) */
+
+typedef struct hsr_draw_desc {
+  hsr_mesh mesh;               /* DrawData::model                                        */
+  int32_t shader;              /* hsr_shader_kind (typeid of DrawData::shader)           */
+  uint32_t flags;              /* HSR_DRAW_*                                             */
+  hsr_texture diffuse;         /* Material::diffuse_map, 0 = none (samples read as zero) */
+  hsr_texture normal;          /* Material::normal_map,  0 = none                        */
+  hsr_target target;           /* DrawData::render_buffer                                */
+  hsr_target shadow_map;       /* ShaderData::shadow_map, 0 = nullptr                    */
+  const hsr_shader_data* uniforms;
+  uint32_t prim_base;          /* prim id written per pixel = prim_base + face + 1       */
+  float clear_depth;           /* used with HSR_DRAW_CLEAR                               */
+  uint8_t clear_rgba[4];       /* used with HSR_DRAW_CLEAR                               */
+} hsr_draw_desc;
+
+/* ---- lifetime ----------------------------------------------------------------------- */
+int hsr_init(int device);                 /* select device, create stream and scratch   */
+int hsr_shutdown(void);                   /* release every handle and device memory     */
+const char* hsr_last_error(void);         /* text of the last failure on this thread    */
+int hsr_abi_version(void);
+
+/* ---- meshes: Model (model.h:8-33) --------------------------------------------------
+ * pos [npos][3], nrm [nnrm][3], uv [nuv][2]; faces [nfaces][3 corners][3] holding the
+ * 0-based (v, vt, vn) index of each corner, the layout of Model::faces_ (model.h:11).
+ * Indices are validated on the host.  Normals are used as stored: the reference
+ * normalises them in place on every access (model.cpp:108-111), which is the identity
+ * for normals that are fixed points of Vector3f::normalize(). */
+int hsr_mesh_upload(const float* pos, int32_t npos, const float* nrm, int32_t nnrm,
+                    const float* uv, int32_t nuv, const int32_t* faces, int32_t nfaces,
+                    hsr_mesh* out);
+/* Replace the normal array of a mesh (same count), e.g. per-corner normals a drop-in
+ * shim extracted through Model::normal(). */
+int hsr_mesh_update_normals(hsr_mesh mesh, const float* nrm, int32_t nnrm);
+int hsr_mesh_release(hsr_mesh mesh);
+
+/* ---- textures: TGAImage (tgaimage.h:66-98) ------------------------------------------
+ * data is the TGAImage buffer: texel (x,y) at (x + y*w)*bytespp, bytes B,G,R(,A);
+ * bytespp in {1,3,4}.  Sampling is TGAImage::get (tgaimage.cpp:248-253). */
+int hsr_texture_upload(const uint8_t* data, int32_t w, int32_t h, int32_t bytespp,
+                       hsr_texture* out);
+int hsr_texture_release(hsr_texture tex);
+
+/* ---- render targets: RenderBuffer (renderbuffer.h:5-22) + a prim-id plane ------------ */
+int hsr_target_create(int32_t w, int32_t h, hsr_target* out);
+int hsr_target_release(hsr_target t);
+int hsr_target_clear(hsr_target t, const uint8_t rgba[4], float depth); /* prim ids -> 0 */
+/* Copy host RenderBuffer contents in (color_buffer RGBA8, depth_buffer FP32); prim may be NULL. */
+int hsr_target_upload(hsr_target t, const uint8_t* rgba, const float* depth, const uint32_t* prim);
+/* Copy out; any pointer may be NULL.  Synchronises with the draws queued before it. */
+int hsr_target_download(hsr_target t, uint8_t* rgba, float* depth, uint32_t* prim);
+
+/* ---- drawing -------------------------------------------------------------------------
+ * hsr_draw: one graphics_draw_triangle() call, queued on the library stream.
+ * hsr_draw_batch: n draws in one launch sequence.  A draw whose shadow_map is the target
+ * of another draw in the batch runs after it (the DrawModel::draw order, scene.h:86-91);
+ * several draws into one target keep their array order. */
+int hsr_draw(const hsr_draw_desc* desc);
+int hsr_draw_batch(const hsr_draw_desc* descs, int32_t n);
+int hsr_synchronize(void);
+
+/* ---- tuning ------------------------------------------------------------------------- */
+typedef struct hsr_tuning {
+  int32_t tile;           /* raster tile edge in pixels: 8, 16 or 32                */
+  int32_t ctas_per_sm;    /* persistent raster CTAs per SM                          */
+  int32_t warps_per_cta;  /* warps per raster CTA (one warp owns one tile)          */
+  float bin_factor;       /* bin capacity = bin_factor * (faces + tiles) pairs      */
+} hsr_tuning;
+int hsr_get_tuning(hsr_tuning* out);
+int hsr_set_tuning(const hsr_tuning* in);
+
+/* ---- statistics of the last completed draw sequence (for tests and benchmarks) ------- */
+typedef struct hsr_stats {
+  uint64_t records;       /* triangles that reached the raster                     */
+  uint64_t clipped_faces; /* faces that went through the homogeneous clipper       */
+  uint64_t bin_pairs;     /* (triangle, tile) pairs                                */
+  uint64_t tiles;         /* tiles visited by the raster                           */
+  uint64_t retries;       /* scratch re-sizes after an overflow                    */
+  uint64_t kernel_launches; /* kernels this library launched since hsr_init         */
+} hsr_stats;
+int hsr_get_stats(hsr_stats* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HSR_H */

@@ -1,0 +1,138 @@
+"""Driver for oracle/_ref/ref_harness — TEST INFRASTRUCTURE ONLY.
+
+Writes a job file (format documented in oracle/ref_harness.cpp), runs the reference's own
+draw path compiled headless, and reads the buffers back.  Used to generate the golden
+fixtures under tests/golden/ and to pin the C restatement (oracle/hsr_oracle.c) against
+the reference where the reference sources are available.
+"""
+from __future__ import annotations
+
+import os
+import struct
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+HARNESS = os.path.join(HERE, "_ref", "ref_harness")
+REF_DIR = "/root/reference/Hana-SoftwareRenderer"
+
+
+def available() -> bool:
+    return os.path.exists(HARNESS)
+
+
+def build() -> bool:
+    """Build oracle/_ref from the read-only reference sources when they are present."""
+    if not os.path.isdir(REF_DIR):
+        return False
+    subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    return available()
+
+
+def _tex_bytes(tex) -> bytes:
+    if tex is None:
+        return struct.pack("<iii", 0, 0, 0)
+    return struct.pack("<iii", tex.w, tex.h, tex.bpp) + np.ascontiguousarray(tex.data).tobytes()
+
+
+def write_job(path: str, frame, obj_path: str, shader: int | None = None) -> None:
+    sw, sh = frame.shadow_size
+    shader = frame.shader if shader is None else shader
+    with open(path, "wb") as f:
+        f.write(b"HSRJOB1\0")
+        f.write(struct.pack("<iiiii", frame.width, frame.height, sw, sh, shader))
+        f.write(struct.pack("<ff", frame.clear_depth, frame.shadow_clear_depth))
+        f.write(bytes(frame.clear_rgba) + bytes(frame.shadow_clear_rgba))
+        f.write(np.ascontiguousarray(frame.sd).tobytes())
+        f.write(_tex_bytes(frame.diffuse))
+        f.write(_tex_bytes(frame.normal))
+        p = obj_path.encode()
+        f.write(struct.pack("<i", len(p)) + p)
+
+
+def read_out(path: str) -> dict:
+    with open(path, "rb") as f:
+        data = f.read()
+    assert data[:8] == b"HSROUT1\0", "bad harness output"
+    off = 8
+    (has_shadow,) = struct.unpack_from("<i", data, off)
+    off += 4
+    out = {}
+    for name in ["main"] + (["shadow"] if has_shadow else []):
+        w, h = struct.unpack_from("<ii", data, off)
+        off += 8
+        depth = np.frombuffer(data, np.float32, w * h, off).reshape(h, w).copy()
+        off += 4 * w * h
+        color = np.frombuffer(data, np.uint8, w * h * 4, off).reshape(h, w, 4).copy()
+        off += 4 * w * h
+        out[name] = {"depth": depth, "color": color}
+    return out
+
+
+def run(frame, shader: int | None = None, obj_mesh=None, workdir: str | None = None) -> dict:
+    """Render one frame with the reference.  ``obj_mesh`` overrides the mesh written to
+    the OBJ (used for the per-face-uv prim-id run)."""
+    from hsr import scenes  # noqa: WPS433 (harness-side import)
+
+    if obj_mesh is None and (frame.shader if shader is None else shader) == scenes.FLAT:
+        obj_mesh = scenes.prim_id_mesh(frame.mesh)  # FLAT == PrimIdShader on per-face uvs
+    own = workdir is None
+    wd = workdir or tempfile.mkdtemp(prefix="hsrref_")
+    try:
+        obj = os.path.join(wd, "mesh.obj")
+        scenes.write_obj(obj_mesh if obj_mesh is not None else frame.mesh, obj)
+        job = os.path.join(wd, "job.bin")
+        out = os.path.join(wd, "out.bin")
+        write_job(job, frame, obj, shader)
+        subprocess.run([HARNESS, "draw", job, out], check=True, stderr=subprocess.DEVNULL)
+        return read_out(out)
+    finally:
+        if own:
+            for n in os.listdir(wd):
+                os.unlink(os.path.join(wd, n))
+            os.rmdir(wd)
+
+
+def run_prim_ids(frame) -> dict:
+    """Reference coverage/depth plus prim ids (face id + 1, 0 = untouched) per pass."""
+    from hsr import scenes
+
+    res = run(frame, shader=8 if frame.shader == scenes.SHADOW else 7, obj_mesh=scenes.prim_id_mesh(frame.mesh))
+    for v in res.values():
+        c = v["color"].astype(np.uint32)
+        v["prim"] = c[:, :, 0] | (c[:, :, 1] << 8) | (c[:, :, 2] << 16)
+    return res
+
+
+def time_frames(frame, frames: int, workdir: str | None = None) -> float:
+    """Milliseconds per frame of the reference on one host core."""
+    from hsr import scenes
+
+    wd = workdir or tempfile.mkdtemp(prefix="hsrref_")
+    obj = os.path.join(wd, "mesh.obj")
+    scenes.write_obj(frame.mesh, obj)
+    job = os.path.join(wd, "job.bin")
+    write_job(job, frame, obj)
+    r = subprocess.run([HARNESS, "time", job, str(frames)], check=True, capture_output=True, text=True)
+    return float(r.stdout.strip())
+
+
+def ref_matrices(eye, target, up, fovy, aspect, near, far, light, ortho) -> dict:
+    """Matrices built by the reference's maths.cpp for the given parameters."""
+    wd = tempfile.mkdtemp(prefix="hsrmat_")
+    try:
+        p = os.path.join(wd, "p.bin")
+        o = os.path.join(wd, "o.bin")
+        vals = list(eye) + list(target) + list(up) + [fovy, aspect, near, far] + list(light) + list(ortho)
+        with open(p, "wb") as f:
+            f.write(np.array(vals, np.float32).tobytes())
+        subprocess.run([HARNESS, "mats", p, o], check=True)
+        a = np.fromfile(o, np.float32)
+        return {"view": a[0:16], "proj": a[16:32], "camera_vp": a[32:48], "light_vp": a[48:64],
+                "model_I": a[64:80], "light_dir": a[80:83]}
+    finally:
+        for n in os.listdir(wd):
+            os.unlink(os.path.join(wd, n))
+        os.rmdir(wd)
