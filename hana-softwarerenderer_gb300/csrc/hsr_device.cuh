@@ -1,0 +1,219 @@
+// hsr_device.cuh — device arithmetic of the draw path.
+//
+// Every float operation is an explicitly rounded intrinsic (__fmul_rn, __fadd_rn, ...),
+// written in the reference's evaluation order, so the compiler can neither contract into
+// FMA nor reassociate: the bits equal the reference's single-precision IEEE arithmetic.
+// Division and square root are the correctly rounded __fdiv_rn / __fsqrt_rn / __dsqrt_rn.
+// std::min / std::max keep their ternary NaN behaviour (no fminf / fmaxf).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "hsr_internal.h"
+
+namespace hsr {
+
+__device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fs(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fd(float a, float b) { return __fdiv_rn(a, b); }
+
+__device__ __forceinline__ float std_min(float a, float b) { return (b < a) ? b : a; }
+__device__ __forceinline__ float std_max(float a, float b) { return (a < b) ? b : a; }
+__device__ __forceinline__ float saturate(float f) { return f < 0.f ? 0.f : (f > 1.f ? 1.f : f); }  // maths.cpp:13-15
+
+// float -> int32 with the meaning x86 cvttss2si gives (truncation; INT_MIN for NaN or
+// out-of-range values), the platform the reference targets.
+__device__ __forceinline__ int32_t cvt_i32(float f) {
+  return (f > -2147483904.0f && f < 2147483648.0f) ? __float2int_rz(f) : (int32_t)0x80000000;
+}
+
+struct F3 { float x, y, z; };
+
+// Vector operator* (vector.h:69-73): ret = 0; ret += a[N-1]*b[N-1]; ... ret += a[0]*b[0].
+__device__ __forceinline__ float dot3(F3 a, F3 b) {
+  float r = fa(0.f, fm(a.z, b.z));
+  r = fa(r, fm(a.y, b.y));
+  return fa(r, fm(a.x, b.x));
+}
+__device__ __forceinline__ float dot4(float a0, float a1, float a2, float a3,
+                                      float b0, float b1, float b2, float b3) {
+  float r = fa(0.f, fm(a3, b3));
+  r = fa(r, fm(a2, b2));
+  r = fa(r, fm(a1, b1));
+  return fa(r, fm(a0, b0));
+}
+__device__ __forceinline__ F3 sub3(F3 a, F3 b) { return {fs(a.x, b.x), fs(a.y, b.y), fs(a.z, b.z)}; }
+__device__ __forceinline__ F3 add3(F3 a, F3 b) { return {fa(a.x, b.x), fa(a.y, b.y), fa(a.z, b.z)}; }
+__device__ __forceinline__ F3 cross3(F3 a, F3 b) {  // vector.h:97-99
+  return {fs(fm(a.y, b.z), fm(a.z, b.y)), fs(fm(a.z, b.x), fm(a.x, b.z)), fs(fm(a.x, b.y), fm(a.y, b.x))};
+}
+__device__ __forceinline__ F3 normalize3(F3 v) {  // vector.h:41-42
+  float n = __fsqrt_rn(fa(fa(fm(v.x, v.x), fm(v.y, v.y)), fm(v.z, v.z)));
+  float f = fd(1.f, n);
+  return {fm(v.x, f), fm(v.y, f), fm(v.z, f)};
+}
+// Matrix4x4 * Vector4f row by row (matrix.h:112-116); m row-major.
+__device__ __forceinline__ float4 mat_vec(const float* m, float x, float y, float z, float w) {
+  return make_float4(dot4(m[0], m[1], m[2], m[3], x, y, z, w), dot4(m[4], m[5], m[6], m[7], x, y, z, w),
+                     dot4(m[8], m[9], m[10], m[11], x, y, z, w), dot4(m[12], m[13], m[14], m[15], x, y, z, w));
+}
+
+// ---- Color (color.cpp:38-64) ------------------------------------------------------------
+struct Col { float r, g, b, a; };
+__device__ __forceinline__ Col c_add(Col a, Col b) {
+  return {std_min(std_max(0.f, fa(a.r, b.r)), 1.f), std_min(std_max(0.f, fa(a.g, b.g)), 1.f),
+          std_min(std_max(0.f, fa(a.b, b.b)), 1.f), std_min(std_max(0.f, fa(a.a, b.a)), 1.f)};
+}
+__device__ __forceinline__ Col c_mulf(Col a, float t) {
+  t = (t > 1.f ? 1.f : (t < 0.f ? 0.f : t));
+  return {std_min(std_max(0.f, fm(a.r, t)), 1.f), std_min(std_max(0.f, fm(a.g, t)), 1.f),
+          std_min(std_max(0.f, fm(a.b, t)), 1.f), std_min(std_max(0.f, fm(a.a, t)), 1.f)};
+}
+__device__ __forceinline__ Col c_mulc(Col a, Col b) { return {fm(a.r, b.r), fm(a.g, b.g), fm(a.b, b.b), fm(a.a, b.a)}; }
+__device__ __forceinline__ Col c_of(const float* p) { return {p[0], p[1], p[2], p[3]}; }
+
+// ---- textures: TGAImage::get (tgaimage.cpp:248-253) on BGRA words ------------------------
+// Texels are stored as 32-bit words b | g<<8 | r<<16 | a<<24 with missing bytes zero,
+// which is what TGAColor(p, bytespp) holds for bytespp 1, 3 and 4.
+__device__ __forceinline__ uint32_t tga_get(const uint32_t* tex, int32_t w, int32_t h, int32_t x, int32_t y) {
+  if (!tex || x < 0 || y < 0 || x >= w || y >= h) return 0u;
+  return __ldg(tex + (size_t)y * (size_t)w + (size_t)x);
+}
+// IShader::tex_diffuse (IShader.h:85-89), Color(TGAColor) (color.cpp:5)
+__device__ __forceinline__ Col tex_diffuse(const DView& v, float u, float t) {
+  uint32_t c = tga_get(v.diffuse, v.dw, v.dh, cvt_i32(fm(u, (float)v.dw)), cvt_i32(fm(t, (float)v.dh)));
+  return {fd((float)((c >> 16) & 255u), 255.f), fd((float)((c >> 8) & 255u), 255.f),
+          fd((float)(c & 255u), 255.f), fd((float)(c >> 24), 255.f)};
+}
+// IShader::tex_normal (IShader.h:91-99)
+__device__ __forceinline__ F3 tex_normal(const DView& v, float u, float t) {
+  uint32_t c = tga_get(v.normal, v.nw, v.nh, cvt_i32(fm(u, (float)v.nw)), cvt_i32(fm(t, (float)v.nh)));
+  F3 r;
+  r.z = fs(fm(fd((float)(c & 255u), 255.f), 2.f), 1.f);
+  r.y = fs(fm(fd((float)((c >> 8) & 255u), 255.f), 2.f), 1.f);
+  r.x = fs(fm(fd((float)((c >> 16) & 255u), 255.f), 2.f), 1.f);
+  return r;
+}
+
+// viewport_transform (maths.cpp:20-25)
+__device__ __forceinline__ F3 viewport(int32_t w, int32_t h, F3 ndc) {
+  return {fm(fm(fa(ndc.x, 1.f), 0.5f), (float)w), fm(fm(fa(ndc.y, 1.f), 0.5f), (float)h), fm(fa(ndc.z, 1.f), 0.5f)};
+}
+
+// IShader::is_in_shadow (IShader.h:107-129).  The shadow map's colour plane may have been
+// written earlier in the same launch by other warps: read it past L1 (ld.global.cg).
+__device__ __forceinline__ int is_in_shadow(const DView& v, float4 dp, float n_dot_l) {
+  if (v.u.enable_shadow && v.sm_color) {
+    float widht = (float)v.smW, height = (float)v.smH;
+    F3 ndc = {fd(dp.x, dp.w), fd(dp.y, dp.w), fd(dp.z, dp.w)};
+    F3 pos = viewport(v.smW, v.smH, ndc);
+    float depth_bias = fm(0.05f, fs(1.f, n_dot_l));
+    if (depth_bias < 0.005f) depth_bias = 0.01f;
+    float current_depth = fs(dp.z, depth_bias);
+    if (pos.x < 0.f || pos.y < 0.f || pos.x >= widht || pos.y >= height) return 1;
+    if (pos.x != pos.x || pos.y != pos.y) return 1;  // NaN: undefined in the reference; lit
+    int32_t x = cvt_i32(pos.x), y = cvt_i32(pos.y);
+    uint32_t word = __ldcg(v.sm_color + (size_t)y * (size_t)v.smW + (size_t)x);
+    float closest_depth = fd((float)(word & 255u), 255.f);
+    return current_depth < closest_depth;
+  }
+  return 1;
+}
+
+// ---- fragment shaders (IShader.cpp) ---------------------------------------------------------
+// Interpolated varyings the fragment stage reads (shader_struct_v2f layout).
+struct Frag {
+  float clip_z;           // [2]
+  F3 wpos;                // [4..6]
+  F3 wnrm;                // [7..9]
+  float u, t;             // [10..11]
+  float intensity;        // [12]
+};
+
+// Blinn-Phong tail shared by BlinnShader and NormalMapShader (IShader.cpp:94-109, :146-162).
+__device__ __forceinline__ Col lit(const DView& v, F3 N, const Frag& f) {
+  const hsr_shader_data& u = v.u;
+  F3 L = {u.light_dir[0], u.light_dir[1], u.light_dir[2]};
+  F3 vp = {u.view_pos[0], u.view_pos[1], u.view_pos[2]};
+  Col albedo = c_mulc(tex_diffuse(v, f.u, f.t), c_of(u.material_color));
+  Col ambient = c_mulc(c_of(u.ambient), albedo);
+  float n_dot_l = saturate(dot3(N, L));
+  Col diffuse = c_mulf(c_mulc(c_of(u.light_color), albedo), n_dot_l);
+  F3 view_dir = normalize3(sub3(vp, f.wpos));
+  F3 half_dir = normalize3(add3(view_dir, L));
+  Col spec = c_mulf(c_mulc(c_of(u.light_color), c_of(u.material_specular)),
+                    powf(saturate(dot3(N, half_dir)), u.gloss));
+  float4 depth_pos = mat_vec(u.light_vp_matrix, f.wpos.x, f.wpos.y, f.wpos.z, 1.f);
+  int shadow = is_in_shadow(v, depth_pos, n_dot_l);
+  return c_add(ambient, c_mulf(c_add(diffuse, spec), (float)shadow));
+}
+
+__device__ __forceinline__ Col fragment(const DView& v, const Frag& f, uint32_t prim) {
+  const Col white = {1.f, 1.f, 1.f, 255.f};
+  switch (v.shader) {
+    case HSR_SHADER_GROUND:  // IShader.cpp:12-15
+      return c_mulf(white, f.intensity);
+    case HSR_SHADER_TOON: {  // IShader.cpp:30-39 (double compares, as written)
+      float intensity = f.intensity;
+      if ((double)intensity > .85) intensity = 1.f;
+      else if ((double)intensity > .60) intensity = (float).80;
+      else if ((double)intensity > .45) intensity = (float).60;
+      else if ((double)intensity > .30) intensity = (float).45;
+      else if ((double)intensity > .15) intensity = (float).30;
+      Col base = {1.f, fd(155.f, 255.f), 0.f, 255.f};
+      return c_mulf(base, intensity);
+    }
+    case HSR_SHADER_TEXTURE:  // IShader.cpp:54-57
+      return tex_diffuse(v, f.u, f.t);
+    case HSR_SHADER_TEXTURE_WITH_LIGHT: {  // IShader.cpp:73-77
+      F3 L = {v.u.light_dir[0], v.u.light_dir[1], v.u.light_dir[2]};
+      return c_mulf(tex_diffuse(v, f.u, f.t), saturate(dot3(f.wnrm, L)));
+    }
+    case HSR_SHADER_BLINN:  // IShader.cpp:94-109
+      return lit(v, normalize3(f.wnrm), f);
+    case HSR_SHADER_NORMALMAP: {  // IShader.cpp:126-162
+      F3 n = f.wnrm;
+      float x = n.x, y = n.y, z = n.z;
+      float sq = __fsqrt_rn(fa(fm(x, x), fm(z, z)));
+      F3 t = {fd(fm(x, y), sq), sq, fd(fm(z, y), sq)};
+      F3 b = cross3(n, t);
+      F3 r0 = {t.x, b.x, n.x}, r1 = {t.y, b.y, n.y}, r2 = {t.z, b.z, n.z};
+      F3 bump = tex_normal(v, f.u, f.t);
+      bump.x = fm(bump.x, v.u.bump_scale);
+      bump.y = fm(bump.y, v.u.bump_scale);
+      float bb = fa(fa(0.f, fm(bump.y, bump.y)), fm(bump.x, bump.x));
+      bump.z = __double2float_rn(__dsqrt_rn(__dsub_rn(1.0, (double)saturate(bb))));
+      F3 tn = {dot3(r0, bump), dot3(r1, bump), dot3(r2, bump)};
+      return lit(v, normalize3(tn), f);
+    }
+    case HSR_SHADER_SHADOW:  // IShader.cpp:176-180
+      return c_mulf(white, f.clip_z);
+    default: {  // FLAT (test shader): bytes of the prim id
+      return {fd(fa((float)(prim & 255u), 0.5f), 255.f), fd(fa((float)((prim >> 8) & 255u), 0.5f), 255.f),
+              fd(fa((float)((prim >> 16) & 255u), 0.5f), 255.f), 255.f};
+    }
+  }
+}
+
+// set_color (renderbuffer.cpp:38-44): R, G, B through (uchar)(c*255); alpha kept.
+__device__ __forceinline__ uint32_t pack_rgb(Col c, uint32_t alpha_word) {
+  uint32_t r = (uint32_t)cvt_i32(fm(c.r, 255.f)) & 255u;
+  uint32_t g = (uint32_t)cvt_i32(fm(c.g, 255.f)) & 255u;
+  uint32_t b = (uint32_t)cvt_i32(fm(c.b, 255.f)) & 255u;
+  return r | (g << 8) | (b << 16) | (alpha_word & 0xFF000000u);
+}
+
+// Varyings each shader reads: which corner streams the shading stage interpolates.
+__device__ __forceinline__ bool needs_wpos(int s) { return s == HSR_SHADER_BLINN || s == HSR_SHADER_NORMALMAP; }
+__device__ __forceinline__ bool needs_wnrm(int s) {
+  return s == HSR_SHADER_GROUND || s == HSR_SHADER_TOON || s == HSR_SHADER_TEXTURE_WITH_LIGHT ||
+         s == HSR_SHADER_BLINN || s == HSR_SHADER_NORMALMAP;
+}
+__device__ __forceinline__ bool needs_uv(int s) {
+  return s == HSR_SHADER_TEXTURE || s == HSR_SHADER_TEXTURE_WITH_LIGHT || s == HSR_SHADER_BLINN ||
+         s == HSR_SHADER_NORMALMAP;
+}
+
+}  // namespace hsr

@@ -1,0 +1,130 @@
+// hsr_internal.h — data layout shared by the host runtime and the sm_103a kernels.
+//
+// Pipeline of one launch sequence (a batch of views = draws):
+//   k_vertex  : SoA attribute streams -> clip / world position / world normal per view
+//   k_setup   : per face: fast accept or homogeneous clip (graphics.cpp:132-161), then per
+//               fan triangle divide / cull / viewport / bbox (graphics.cpp:314-347) -> one
+//               64-byte RasterRec, plus per-tile counts (warp-aggregated atomics)
+//   k_scan    : exclusive prefix sum of the per-tile counts (decoupled look-back)
+//   k_scatter : (record, tile) pairs into per-tile lists
+//   k_raster  : persistent; one warp owns one screen tile, resolves visibility per pixel
+//               as min over (depth, later-submitted) — the sequential loop's result —
+//               then shades the winners and writes colour / depth / prim id once.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/hsr.h"
+
+namespace hsr {
+
+constexpr int kMaxPoly = 10;              // 3 vertices + one per clip plane (7 planes)
+constexpr int kVaryings = 13;             // floats in shader_struct_v2f (IShader.h:41-47)
+constexpr int kClipSlotFloats = 4 + kMaxPoly * kVaryings + 2;  // n, pad[3], verts, pad -> 136
+constexpr int kBigRecordTiles = 32;       // records touching more tiles are binned by a warp
+
+// Error bits in Ctl::error.
+enum : uint32_t {
+  kErrRecOverflow = 1u,
+  kErrClipOverflow = 2u,
+  kErrBinOverflow = 4u,
+  kErrWaitTimeout = 8u,
+  kErrScanTimeout = 16u,
+};
+
+// Record flags.
+enum : uint32_t {
+  kRecExact = 1u,  // coordinates outside the range where the division-free coverage test is
+                   // exact: the raster evaluates the reference's divisions instead
+};
+
+// One triangle that reached the raster (64 bytes).  A, B-A, C-A are the per-triangle
+// constants of barycentric() (graphics.cpp:222-233); uz is u.z, constant per triangle.
+struct __align__(16) RasterRec {
+  float ax, ay, e1x, e1y;   // A; e1 = B - A
+  float e2x, e2y, uz, d0;   // e2 = C - A; u.z; screen depth of A
+  float d1, d2;             // screen depths of B, C
+  uint32_t seq;             // (face << 4) | (fan << 1) | clipped — submission order
+  uint32_t view;            // index of the view in the batch
+  uint32_t xr, yr;          // inclusive pixel range: x0 | x1 << 16, y0 | y1 << 16
+  uint32_t flags, pad;
+};
+static_assert(sizeof(RasterRec) == 64, "RasterRec must stay 64 bytes");
+
+// Per-draw descriptor on the device.
+struct DView {
+  // mesh (device)
+  const float* px; const float* py; const float* pz;   // positions, SoA, padded to 4
+  const float* nx; const float* ny; const float* nz;   // normals, SoA, padded to 4
+  const float2* uv;
+  const int4* fv; const int4* fvt; const int4* fvn;    // per-face corner indices (+pad)
+  int32_t npos, nnrm, nuv, nfaces;
+  // vertex outputs (scratch)
+  float4* clip;   // [npos]
+  float4* wpos;   // [npos] or null
+  float4* wnrm;   // [nnrm] (xyz, intensity) or null
+  int32_t* clip_slot;  // [nfaces]: slot in the clip buffer, written for clipped faces only
+  // shading
+  int32_t shader;
+  uint32_t flags;       // HSR_DRAW_*
+  float mvp[16];        // camera_vp*model (light_vp*model for SHADOW), host-computed
+  hsr_shader_data u;
+  const uint32_t* diffuse; int32_t dw, dh, dbpp;
+  const uint32_t* normal;  int32_t nw, nh, nbpp;
+  // target
+  uint32_t* color; float* depth; uint32_t* prim; int32_t W, H;
+  // shadow map (colour plane of another target), null when ShaderData::shadow_map is null
+  const uint32_t* sm_color; int32_t smW, smH;
+  // ordering inside the batch: views this one waits for (-1 = none)
+  int32_t dep0, dep1;
+  // tiles
+  int32_t tile_base, tiles_x, tiles_y, ntiles;
+  uint32_t prim_base;
+  float clear_depth;
+  uint32_t clear_rgba;
+};
+
+struct Ctl {
+  uint32_t rec_count;
+  uint32_t clip_count;
+  uint32_t tile_next;
+  uint32_t scan_ticket;
+  uint32_t error;
+  uint32_t bin_total;
+  uint32_t raster_tiles;
+  uint32_t pad;
+};
+
+// Work chunk for the vertex and setup kernels: items [begin, end) of one view.
+struct Chunk {
+  int32_t view;
+  int32_t kind;   // vertex kernel: 0 = positions, 1 = normals
+  int32_t begin;
+  int32_t end;
+};
+
+// Scratch of one launch sequence (device pointers, sized by the host).
+struct Scratch {
+  Ctl* ctl;
+  uint32_t* view_done;      // [nviews] tiles finished per view
+  RasterRec* recs;  uint32_t rec_cap;
+  float* clipbuf;   uint32_t clip_cap;   // kClipSlotFloats per slot
+  uint32_t* tile_count;     // [ntiles]
+  uint32_t* tile_fill;      // [ntiles]
+  uint32_t* tile_off;       // [ntiles]
+  unsigned long long* scan_status;  // [scan blocks]
+  uint32_t* bins;   uint32_t bin_cap;
+  int32_t ntiles;
+  int32_t nviews;
+};
+
+// Kernel launchers (kernels_*.cu).  All return cudaError_t as int.
+int launch_vertex(const DView* views, const Chunk* chunks, int nchunks, cudaStream_t s);
+int launch_setup(const DView* views, const Chunk* chunks, int nchunks, int tile, Scratch sc, cudaStream_t s);
+int launch_scan(Scratch sc, cudaStream_t s);
+int launch_scatter(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s);
+int launch_raster(const DView* views, int tile, Scratch sc, int grid, int warps, cudaStream_t s);
+int scan_blocks(int ntiles);
+
+}  // namespace hsr

@@ -1,0 +1,654 @@
+// hsr_runtime.cu — host runtime and C ABI (include/hsr.h).
+//
+// Replaces graphics_draw_triangle(DrawData*) (graphics.h:15, graphics.cpp:378-407) by
+// handle-based calls.  Meshes, textures and targets live in device memory; hsr_draw_batch
+// turns a list of draws into one launch sequence (vertex, setup, scan, scatter, raster)
+// over all of them.  Scratch is a grow-only arena; an overflow detected on the device
+// leaves the targets untouched (the raster checks the error word first) and the batch is
+// re-run with larger capacity.  No CPU fallback exists: without a device every call
+// fails with a status code.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "hsr_internal.h"
+#include "hsr_runtime.h"
+
+namespace hsr {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+int cuda_fail(cudaError_t e, const char* where) {
+  g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
+  return HSR_ERR_CUDA;
+}
+
+Runtime* g_rt = nullptr;
+std::mutex g_mu;
+
+// ---- small helpers --------------------------------------------------------------------
+static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Matrix product in the reference's order: out[i][j] = a[i] . col_j(b), accumulated from
+// index 3 down (matrix.h:118-123, vector.h:69-73).  Host code is built without FP
+// contraction, so these are plain IEEE single-precision operations.
+void mat_mul_ref(const float* a, const float* b, float* out) {
+  for (int i = 0; i < 4; i++)
+    for (int j = 0; j < 4; j++) {
+      float r = 0.f;
+      for (int k = 3; k >= 0; k--) {
+        float p = a[i * 4 + k] * b[k * 4 + j];
+        r = r + p;
+      }
+      out[i * 4 + j] = r;
+    }
+}
+
+// ---- device buffers ---------------------------------------------------------------------
+static int dalloc(void** p, size_t bytes, const char* what) {
+  *p = nullptr;
+  if (bytes == 0) return HSR_OK;
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(HSR_ERR_OUT_OF_MEMORY, std::string("cudaMalloc failed for ") + what + ": " + cudaGetErrorString(e));
+  }
+  return HSR_OK;
+}
+
+MeshObj::~MeshObj() {
+  for (void* p : {(void*)px, (void*)py, (void*)pz, (void*)nx, (void*)ny, (void*)nz, (void*)uv, (void*)fv,
+                  (void*)fvt, (void*)fvn})
+    if (p) cudaFree(p);
+}
+TexObj::~TexObj() {
+  if (words) cudaFree(words);
+}
+TargetObj::~TargetObj() {
+  if (color) cudaFree(color);
+  if (depth) cudaFree(depth);
+  if (prim) cudaFree(prim);
+}
+
+int Arena::reserve(size_t bytes) {
+  if (bytes <= cap) return HSR_OK;
+  const size_t want = std::max(bytes, cap + cap / 2);
+  if (base) cudaFree(base);
+  base = nullptr;
+  cap = 0;
+  int rc = dalloc((void**)&base, want, "scratch arena");
+  if (rc != HSR_OK) return rc;
+  cap = want;
+  return HSR_OK;
+}
+
+int Pinned::reserve(size_t bytes) {
+  if (bytes <= cap) return HSR_OK;
+  if (base) cudaFreeHost(base);
+  base = nullptr;
+  cap = 0;
+  size_t want = std::max(bytes, (size_t)1 << 16);
+  cudaError_t e = cudaMallocHost((void**)&base, want);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(HSR_ERR_OUT_OF_MEMORY, "cudaMallocHost failed");
+  }
+  cap = want;
+  return HSR_OK;
+}
+
+template <class T> T* Runtime::get(std::unordered_map<uint64_t, T*>& m, uint64_t h) {
+  auto it = m.find(h);
+  return it == m.end() ? nullptr : it->second;
+}
+
+MeshObj* Runtime::mesh(uint64_t h) { return get(meshes, h); }
+TexObj* Runtime::tex(uint64_t h) { return get(textures, h); }
+TargetObj* Runtime::target(uint64_t h) { return get(targets, h); }
+
+// ---- batch planning -----------------------------------------------------------------------
+static bool shader_needs_wpos(int s) { return s == HSR_SHADER_BLINN || s == HSR_SHADER_NORMALMAP; }
+static bool shader_needs_wnrm(int s) {
+  return s == HSR_SHADER_GROUND || s == HSR_SHADER_TOON || s == HSR_SHADER_TEXTURE_WITH_LIGHT ||
+         s == HSR_SHADER_BLINN || s == HSR_SHADER_NORMALMAP;
+}
+
+int Runtime::validate(const hsr_draw_desc& d) {
+  if (!d.uniforms) return fail(HSR_ERR_INVALID_ARG, "draw: uniforms is null");
+  if (d.shader < 0 || d.shader >= HSR_SHADER_COUNT) return fail(HSR_ERR_UNKNOWN_SHADER, "draw: unknown shader kind");
+  if (!mesh(d.mesh)) return fail(HSR_ERR_BAD_HANDLE, "draw: unknown mesh handle");
+  if (!target(d.target)) return fail(HSR_ERR_BAD_HANDLE, "draw: unknown target handle");
+  if (d.diffuse && !tex(d.diffuse)) return fail(HSR_ERR_BAD_HANDLE, "draw: unknown diffuse texture handle");
+  if (d.normal && !tex(d.normal)) return fail(HSR_ERR_BAD_HANDLE, "draw: unknown normal texture handle");
+  if (d.shadow_map && !target(d.shadow_map)) return fail(HSR_ERR_BAD_HANDLE, "draw: unknown shadow_map handle");
+  if (d.shadow_map && d.shadow_map == d.target) return fail(HSR_ERR_INVALID_ARG, "draw: shadow_map is the target itself");
+  return HSR_OK;
+}
+
+// Order the draws: a consumer of a shadow map waits for the draw that renders it; draws into
+// one target keep their array order.  Returns levels via topological order.
+int Runtime::plan_order(const hsr_draw_desc* d, int n, std::vector<int>& order, std::vector<int>& dep0,
+                        std::vector<int>& dep1) {
+  dep0.assign(n, -1);
+  dep1.assign(n, -1);
+  for (int i = 0; i < n; i++) {
+    if (d[i].shadow_map) {
+      for (int j = n - 1; j >= 0; j--)
+        if (j != i && d[j].target == d[i].shadow_map) { dep0[i] = j; break; }
+    }
+    for (int j = i - 1; j >= 0; j--)
+      if (d[j].target == d[i].target) { dep1[i] = j; break; }
+  }
+  std::vector<int> level(n, -1);
+  // longest-path levels with cycle detection (n is small)
+  for (int iter = 0; iter <= n; iter++) {
+    bool changed = false;
+    for (int i = 0; i < n; i++) {
+      int l = 0;
+      for (int dp : {dep0[i], dep1[i]})
+        if (dp >= 0) l = std::max(l, level[dp] < 0 ? 1 : level[dp] + 1);
+      if (l != level[i]) { level[i] = l; changed = true; }
+    }
+    if (!changed) break;
+    if (iter == n) return fail(HSR_ERR_INVALID_ARG, "draw batch: circular shadow-map / target dependencies");
+  }
+  order.resize(n);
+  for (int i = 0; i < n; i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return level[a] < level[b]; });
+  return HSR_OK;
+}
+
+int Runtime::run_batch(const hsr_draw_desc* descs, int n) {
+  if (n <= 0) return HSR_OK;
+  for (int i = 0; i < n; i++) {
+    int rc = validate(descs[i]);
+    if (rc != HSR_OK) return rc;
+  }
+  std::vector<int> order, dep0, dep1;
+  int rc = plan_order(descs, n, order, dep0, dep1);
+  if (rc != HSR_OK) return rc;
+  std::vector<int> pos(n);
+  for (int k = 0; k < n; k++) pos[order[k]] = k;
+
+  const int T = tuning.tile;
+  // ---- host-side view descriptors and scratch layout --------------------------------
+  std::vector<DView> views(n);
+  std::vector<Chunk> vchunks, schunks;
+  size_t total_faces = 0, total_tiles = 0;
+  struct Off { size_t clip, wpos, wnrm, slot; };
+  std::vector<Off> offs(n);
+  size_t bytes = 0;
+  for (int k = 0; k < n; k++) {
+    const hsr_draw_desc& d = descs[order[k]];
+    MeshObj* m = mesh(d.mesh);
+    TargetObj* tg = target(d.target);
+    DView& v = views[k];
+    std::memset(&v, 0, sizeof(v));
+    v.px = m->px; v.py = m->py; v.pz = m->pz;
+    v.nx = m->nx; v.ny = m->ny; v.nz = m->nz;
+    v.uv = m->uv;
+    v.fv = m->fv; v.fvt = m->fvt; v.fvn = m->fvn;
+    v.npos = m->npos; v.nnrm = m->nnrm; v.nuv = m->nuv; v.nfaces = m->nfaces;
+    v.shader = d.shader;
+    v.flags = d.flags;
+    v.u = *d.uniforms;
+    mat_mul_ref(d.shader == HSR_SHADER_SHADOW ? v.u.light_vp_matrix : v.u.camera_vp_matrix, v.u.model_matrix, v.mvp);
+    if (d.diffuse) {
+      TexObj* t = tex(d.diffuse);
+      v.diffuse = t->words; v.dw = t->w; v.dh = t->h; v.dbpp = t->bpp;
+    }
+    if (d.normal) {
+      TexObj* t = tex(d.normal);
+      v.normal = t->words; v.nw = t->w; v.nh = t->h; v.nbpp = t->bpp;
+    }
+    v.color = tg->color; v.depth = tg->depth; v.prim = tg->prim; v.W = tg->w; v.H = tg->h;
+    if (d.shadow_map) {
+      TargetObj* sm = target(d.shadow_map);
+      v.sm_color = sm->color; v.smW = sm->w; v.smH = sm->h;
+    }
+    v.dep0 = dep0[order[k]] >= 0 ? pos[dep0[order[k]]] : -1;
+    v.dep1 = dep1[order[k]] >= 0 ? pos[dep1[order[k]]] : -1;
+    v.tiles_x = (tg->w + T - 1) / T;
+    v.tiles_y = (tg->h + T - 1) / T;
+    v.ntiles = v.tiles_x * v.tiles_y;
+    v.tile_base = (int32_t)total_tiles;
+    v.prim_base = d.prim_base;
+    v.clear_depth = d.clear_depth;
+    std::memcpy(&v.clear_rgba, d.clear_rgba, 4);
+    total_tiles += (size_t)v.ntiles;
+    total_faces += (size_t)m->nfaces;
+    Off& o = offs[k];
+    o.clip = bytes; bytes = align_up(bytes + sizeof(float4) * (size_t)std::max(m->npos, 1), 256);
+    o.wpos = bytes; if (shader_needs_wpos(d.shader)) bytes = align_up(bytes + sizeof(float4) * (size_t)std::max(m->npos, 1), 256);
+    o.wnrm = bytes; if (shader_needs_wnrm(d.shader)) bytes = align_up(bytes + sizeof(float4) * (size_t)std::max(m->nnrm, 1), 256);
+    o.slot = bytes; bytes = align_up(bytes + sizeof(int32_t) * (size_t)std::max(m->nfaces, 1), 256);
+    for (int b = 0; b < m->npos; b += 1024) vchunks.push_back({k, 0, b, std::min(m->npos, b + 1024)});
+    if (shader_needs_wnrm(d.shader))
+      for (int b = 0; b < m->nnrm; b += 1024) vchunks.push_back({k, 1, b, std::min(m->nnrm, b + 1024)});
+    for (int b = 0; b < m->nfaces; b += 256) schunks.push_back({k, 0, b, std::min(m->nfaces, b + 256)});
+  }
+  if (total_tiles > (size_t)INT32_MAX) return fail(HSR_ERR_INVALID_ARG, "draw batch: too many tiles");
+  const size_t view_bytes = bytes;
+
+  // capacities (grow on overflow, remembered across calls)
+  size_t rec_cap = std::max<size_t>(cap_rec_hint, total_faces + total_faces / 4 + 1024);
+  size_t clip_cap = std::max<size_t>(cap_clip_hint, total_faces / 16 + 256);
+  size_t bin_cap = std::max<size_t>(cap_bin_hint, (size_t)(tuning.bin_factor * (double)(total_faces + total_tiles)) + 4096);
+
+  for (int attempt = 0; attempt < 6; attempt++) {
+    rec_cap = std::min<size_t>(rec_cap, 0xfffff000u);
+    clip_cap = std::min<size_t>(clip_cap, 0xfffff000u);
+    bin_cap = std::min<size_t>(bin_cap, 0xfffff000u);
+    const int nscan = scan_blocks((int)total_tiles);
+    // layout: [views | chunks | per-view vertex outputs | ctl | view_done | tile_count |
+    //          tile_fill | scan_status | tile_off | recs | clipbuf | bins]
+    size_t off = 0;
+    const size_t o_views = off; off = align_up(off + sizeof(DView) * n, 256);
+    const size_t o_vch = off; off = align_up(off + sizeof(Chunk) * std::max<size_t>(vchunks.size(), 1), 256);
+    const size_t o_sch = off; off = align_up(off + sizeof(Chunk) * std::max<size_t>(schunks.size(), 1), 256);
+    const size_t o_vout = off; off = align_up(off + view_bytes, 256);
+    const size_t o_zero = off;
+    const size_t o_ctl = off; off = align_up(off + sizeof(Ctl), 256);
+    const size_t o_done = off; off = align_up(off + sizeof(uint32_t) * n, 256);
+    const size_t o_cnt = off; off = align_up(off + sizeof(uint32_t) * total_tiles, 256);
+    const size_t o_fill = off; off = align_up(off + sizeof(uint32_t) * total_tiles, 256);
+    const size_t o_stat = off; off = align_up(off + sizeof(unsigned long long) * std::max(nscan, 1), 256);
+    const size_t zero_bytes = off - o_zero;
+    const size_t o_toff = off; off = align_up(off + sizeof(uint32_t) * total_tiles, 256);
+    const size_t o_recs = off; off = align_up(off + sizeof(RasterRec) * rec_cap, 256);
+    const size_t o_clip = off; off = align_up(off + sizeof(float) * kClipSlotFloats * clip_cap, 256);
+    const size_t o_bins = off; off = align_up(off + sizeof(uint32_t) * bin_cap, 256);
+    int rc2 = arena.reserve(off);
+    if (rc2 != HSR_OK) return rc2;
+    char* B = arena.base;
+    for (int k = 0; k < n; k++) {
+      DView& v = views[k];
+      v.clip = (float4*)(B + o_vout + offs[k].clip);
+      v.wpos = shader_needs_wpos(v.shader) ? (float4*)(B + o_vout + offs[k].wpos) : nullptr;
+      v.wnrm = shader_needs_wnrm(v.shader) ? (float4*)(B + o_vout + offs[k].wnrm) : nullptr;
+      v.clip_slot = (int32_t*)(B + o_vout + offs[k].slot);
+    }
+    const size_t host_bytes = o_vout;
+    rc2 = staging.reserve(host_bytes + sizeof(Ctl));
+    if (rc2 != HSR_OK) return rc2;
+    std::memcpy(staging.base + o_views, views.data(), sizeof(DView) * n);
+    if (!vchunks.empty()) std::memcpy(staging.base + o_vch, vchunks.data(), sizeof(Chunk) * vchunks.size());
+    if (!schunks.empty()) std::memcpy(staging.base + o_sch, schunks.data(), sizeof(Chunk) * schunks.size());
+
+    Scratch sc;
+    sc.ctl = (Ctl*)(B + o_ctl);
+    sc.view_done = (uint32_t*)(B + o_done);
+    sc.recs = (RasterRec*)(B + o_recs); sc.rec_cap = (uint32_t)rec_cap;
+    sc.clipbuf = (float*)(B + o_clip); sc.clip_cap = (uint32_t)clip_cap;
+    sc.tile_count = (uint32_t*)(B + o_cnt);
+    sc.tile_fill = (uint32_t*)(B + o_fill);
+    sc.tile_off = (uint32_t*)(B + o_toff);
+    sc.scan_status = (unsigned long long*)(B + o_stat);
+    sc.bins = (uint32_t*)(B + o_bins); sc.bin_cap = (uint32_t)bin_cap;
+    sc.ntiles = (int32_t)total_tiles;
+    sc.nviews = n;
+
+    const DView* dviews = (const DView*)(B + o_views);
+    cudaError_t e = cudaMemcpyAsync(B, staging.base, host_bytes, cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) return cuda_fail(e, "upload views");
+    e = cudaMemsetAsync(B + o_zero, 0, zero_bytes, stream);
+    if (e != cudaSuccess) return cuda_fail(e, "clear scratch");
+    int kr = launch_vertex(dviews, (const Chunk*)(B + o_vch), (int)vchunks.size(), stream);
+    if (kr) return cuda_fail((cudaError_t)kr, "vertex kernel");
+    kr = launch_setup(dviews, (const Chunk*)(B + o_sch), (int)schunks.size(), T, sc, stream);
+    if (kr) return cuda_fail((cudaError_t)kr, "setup kernel");
+    kr = launch_scan(sc, stream);
+    if (kr) return cuda_fail((cudaError_t)kr, "scan kernel");
+    kr = launch_scatter(dviews, T, sc, num_sms * 4, stream);
+    if (kr) return cuda_fail((cudaError_t)kr, "scatter kernel");
+    kr = launch_raster(dviews, T, sc, num_sms * tuning.ctas_per_sm, tuning.warps_per_cta, stream);
+    if (kr) return cuda_fail((cudaError_t)kr, "raster kernel");
+    launches += (vchunks.empty() ? 0 : 1) + (schunks.empty() ? 0 : 1) + (nscan > 0 ? 1 : 0) + 2;
+    Ctl* hctl = (Ctl*)(staging.base + host_bytes);
+    e = cudaMemcpyAsync(hctl, sc.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, stream);
+    if (e != cudaSuccess) return cuda_fail(e, "read control block");
+    e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return cuda_fail(e, "draw batch");
+    const Ctl c = *hctl;
+    if (c.error & (kErrRecOverflow | kErrClipOverflow | kErrBinOverflow)) {
+      if (c.error & kErrRecOverflow) rec_cap = std::max<size_t>(rec_cap * 2, (size_t)c.rec_count + 1024);
+      if (c.error & kErrClipOverflow) clip_cap = std::max<size_t>(clip_cap * 2, (size_t)c.clip_count + 256);
+      if (c.error & kErrBinOverflow) bin_cap = std::max<size_t>(bin_cap * 2, (size_t)c.bin_total + 4096);
+      stats.retries++;
+      cap_rec_hint = rec_cap; cap_clip_hint = clip_cap; cap_bin_hint = bin_cap;
+      continue;
+    }
+    if (c.error & (kErrWaitTimeout | kErrScanTimeout))
+      return fail(HSR_ERR_TIMEOUT, "draw batch: a bounded device wait gave up");
+    stats.records = c.rec_count;
+    stats.clipped_faces = c.clip_count;
+    stats.bin_pairs = c.bin_total;
+    stats.tiles = c.raster_tiles;
+    stats.kernel_launches = launches;
+    return HSR_OK;
+  }
+  return fail(HSR_ERR_BIN_OVERFLOW, "draw batch: scratch overflow persisted after retries");
+}
+
+// renderbuffer_clear_color / renderbuffer_clear_depth (renderbuffer.cpp:59-75) with the
+// colour given as bytes; prim ids -> 0.
+__global__ void k_clear(uint32_t* __restrict__ color, float* __restrict__ depth, uint32_t* __restrict__ prim,
+                        size_t n, uint32_t rgba, float d) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    color[i] = rgba;
+    depth[i] = d;
+    if (prim) prim[i] = 0u;
+  }
+}
+
+int launch_clear(uint32_t* color, float* depth, uint32_t* prim, size_t n, uint32_t rgba, float d, cudaStream_t s) {
+  const int grid = (int)std::min<size_t>((n + 255) / 256, 4096);
+  k_clear<<<std::max(grid, 1), 256, 0, s>>>(color, depth, prim, n, rgba, d);
+  return (int)cudaGetLastError();
+}
+
+int Runtime::clear_target(TargetObj* t, const uint8_t rgba[4], float depth) {
+  uint32_t word;
+  std::memcpy(&word, rgba, 4);
+  int kr = launch_clear(t->color, t->depth, t->prim, (size_t)t->w * (size_t)t->h, word, depth, stream);
+  if (kr) return cuda_fail((cudaError_t)kr, "clear kernel");
+  launches++;
+  cudaError_t e = cudaStreamSynchronize(stream);
+  return e == cudaSuccess ? HSR_OK : cuda_fail(e, "clear");
+}
+
+}  // namespace hsr
+
+using namespace hsr;
+
+#define RT_OR_FAIL()                                                                \
+  std::lock_guard<std::mutex> lock_(g_mu);                                          \
+  if (!g_rt) return fail(HSR_ERR_NOT_INITIALIZED, "hsr_init() has not succeeded")
+
+extern "C" {
+
+int hsr_abi_version(void) { return HSR_ABI_VERSION; }
+
+const char* hsr_last_error(void) { return g_last_error.c_str(); }
+
+int hsr_init(int device) {
+  std::lock_guard<std::mutex> lock(g_mu);
+  if (g_rt) return HSR_OK;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return fail(HSR_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+  }
+  if (device < 0 || device >= count) return fail(HSR_ERR_INVALID_ARG, "hsr_init: device index out of range");
+  e = cudaSetDevice(device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  Runtime* rt = new Runtime();
+  rt->device = device;
+  cudaDeviceProp prop;
+  e = cudaGetDeviceProperties(&prop, device);
+  if (e != cudaSuccess) { delete rt; return cuda_fail(e, "cudaGetDeviceProperties"); }
+  rt->num_sms = prop.multiProcessorCount;
+  e = cudaStreamCreateWithFlags(&rt->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { delete rt; return cuda_fail(e, "cudaStreamCreate"); }
+  g_rt = rt;
+  return HSR_OK;
+}
+
+int hsr_shutdown(void) {
+  std::lock_guard<std::mutex> lock(g_mu);
+  if (!g_rt) return HSR_OK;
+  cudaStreamSynchronize(g_rt->stream);
+  for (auto& kv : g_rt->meshes) delete kv.second;
+  for (auto& kv : g_rt->textures) delete kv.second;
+  for (auto& kv : g_rt->targets) delete kv.second;
+  if (g_rt->arena.base) cudaFree(g_rt->arena.base);
+  if (g_rt->staging.base) cudaFreeHost(g_rt->staging.base);
+  cudaStreamDestroy(g_rt->stream);
+  delete g_rt;
+  g_rt = nullptr;
+  return HSR_OK;
+}
+
+int hsr_mesh_upload(const float* pos, int32_t npos, const float* nrm, int32_t nnrm, const float* uv, int32_t nuv,
+                    const int32_t* faces, int32_t nfaces, hsr_mesh* out) {
+  RT_OR_FAIL();
+  if (!out || npos < 0 || nnrm < 0 || nuv < 0 || nfaces < 0) return fail(HSR_ERR_INVALID_ARG, "mesh: bad arguments");
+  if (nfaces > (1 << 27)) return fail(HSR_ERR_INVALID_ARG, "mesh: more than 2^27 faces");
+  if ((npos && !pos) || (nnrm && !nrm) || (nuv && !uv) || (nfaces && !faces))
+    return fail(HSR_ERR_INVALID_ARG, "mesh: null array with nonzero count");
+  for (int64_t i = 0; i < (int64_t)nfaces * 3; i++) {
+    const int32_t* c = faces + i * 3;
+    if (c[0] < 0 || c[0] >= npos || c[1] < 0 || c[1] >= nuv || c[2] < 0 || c[2] >= nnrm)
+      return fail(HSR_ERR_INVALID_ARG, "mesh: face index out of range (face " + std::to_string(i / 3) + ")");
+  }
+  MeshObj* m = new MeshObj();
+  m->npos = npos; m->nnrm = nnrm; m->nuv = nuv; m->nfaces = nfaces;
+  const size_t P = align_up((size_t)std::max(npos, 1), 4), N = align_up((size_t)std::max(nnrm, 1), 4);
+  std::vector<float> tmp(std::max(P, N), 0.f);
+  int rc = HSR_OK;
+  auto up_soa = [&](const float* src, int cnt, int comp, size_t padded, float** dst) -> int {
+    int r = dalloc((void**)dst, sizeof(float) * padded, "mesh");
+    if (r != HSR_OK) return r;
+    std::fill(tmp.begin(), tmp.begin() + padded, 0.f);
+    for (int i = 0; i < cnt; i++) tmp[i] = src[(size_t)i * 3 + comp];
+    cudaError_t e = cudaMemcpy(*dst, tmp.data(), sizeof(float) * padded, cudaMemcpyHostToDevice);
+    return e == cudaSuccess ? HSR_OK : cuda_fail(e, "mesh upload");
+  };
+  for (int c = 0; c < 3 && rc == HSR_OK; c++) rc = up_soa(pos, npos, c, P, c == 0 ? &m->px : (c == 1 ? &m->py : &m->pz));
+  for (int c = 0; c < 3 && rc == HSR_OK; c++) rc = up_soa(nrm, nnrm, c, N, c == 0 ? &m->nx : (c == 1 ? &m->ny : &m->nz));
+  if (rc == HSR_OK) rc = dalloc((void**)&m->uv, sizeof(float2) * (size_t)std::max(nuv, 1), "mesh uv");
+  if (rc == HSR_OK && nuv) {
+    cudaError_t e = cudaMemcpy(m->uv, uv, sizeof(float2) * (size_t)nuv, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) rc = cuda_fail(e, "mesh uv upload");
+  }
+  if (rc == HSR_OK) {
+    const size_t F = (size_t)std::max(nfaces, 1);
+    std::vector<int4> fv(F), ft(F), fn(F);
+    for (int i = 0; i < nfaces; i++) {
+      const int32_t* f = faces + (size_t)i * 9;
+      fv[i] = make_int4(f[0], f[3], f[6], 0);
+      ft[i] = make_int4(f[1], f[4], f[7], 0);
+      fn[i] = make_int4(f[2], f[5], f[8], 0);
+    }
+    int4** dsts[3] = {&m->fv, &m->fvt, &m->fvn};
+    std::vector<int4>* srcs[3] = {&fv, &ft, &fn};
+    for (int k = 0; k < 3 && rc == HSR_OK; k++) {
+      rc = dalloc((void**)dsts[k], sizeof(int4) * F, "mesh faces");
+      if (rc == HSR_OK) {
+        cudaError_t e = cudaMemcpy(*dsts[k], srcs[k]->data(), sizeof(int4) * F, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) rc = cuda_fail(e, "mesh faces upload");
+      }
+    }
+  }
+  if (rc != HSR_OK) { delete m; return rc; }
+  const uint64_t h = g_rt->next_handle++;
+  g_rt->meshes[h] = m;
+  *out = h;
+  return HSR_OK;
+}
+
+int hsr_mesh_update_normals(hsr_mesh mh, const float* nrm, int32_t nnrm) {
+  RT_OR_FAIL();
+  MeshObj* m = g_rt->mesh(mh);
+  if (!m) return fail(HSR_ERR_BAD_HANDLE, "mesh_update_normals: unknown mesh");
+  if (nnrm != m->nnrm || (nnrm && !nrm)) return fail(HSR_ERR_INVALID_ARG, "mesh_update_normals: count mismatch");
+  cudaStreamSynchronize(g_rt->stream);
+  const size_t N = align_up((size_t)std::max(nnrm, 1), 4);
+  std::vector<float> tmp(N, 0.f);
+  float* dst[3] = {m->nx, m->ny, m->nz};
+  for (int c = 0; c < 3; c++) {
+    for (int i = 0; i < nnrm; i++) tmp[i] = nrm[(size_t)i * 3 + c];
+    cudaError_t e = cudaMemcpy(dst[c], tmp.data(), sizeof(float) * N, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "normal upload");
+  }
+  return HSR_OK;
+}
+
+int hsr_mesh_release(hsr_mesh mh) {
+  RT_OR_FAIL();
+  auto it = g_rt->meshes.find(mh);
+  if (it == g_rt->meshes.end()) return fail(HSR_ERR_BAD_HANDLE, "mesh_release: unknown mesh");
+  cudaStreamSynchronize(g_rt->stream);
+  delete it->second;
+  g_rt->meshes.erase(it);
+  return HSR_OK;
+}
+
+int hsr_texture_upload(const uint8_t* data, int32_t w, int32_t h, int32_t bytespp, hsr_texture* out) {
+  RT_OR_FAIL();
+  if (!out || !data || w <= 0 || h <= 0 || (bytespp != 1 && bytespp != 3 && bytespp != 4))
+    return fail(HSR_ERR_INVALID_ARG, "texture: bad arguments (bytespp must be 1, 3 or 4)");
+  const size_t n = (size_t)w * (size_t)h;
+  std::vector<uint32_t> words(n);
+  for (size_t i = 0; i < n; i++) {
+    uint32_t wv = 0;
+    for (int k = 0; k < bytespp; k++) wv |= (uint32_t)data[i * bytespp + k] << (8 * k);
+    words[i] = wv;
+  }
+  TexObj* t = new TexObj();
+  t->w = w; t->h = h; t->bpp = bytespp;
+  int rc = dalloc((void**)&t->words, sizeof(uint32_t) * n, "texture");
+  if (rc == HSR_OK) {
+    cudaError_t e = cudaMemcpy(t->words, words.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) rc = cuda_fail(e, "texture upload");
+  }
+  if (rc != HSR_OK) { delete t; return rc; }
+  const uint64_t hd = g_rt->next_handle++;
+  g_rt->textures[hd] = t;
+  *out = hd;
+  return HSR_OK;
+}
+
+int hsr_texture_release(hsr_texture th) {
+  RT_OR_FAIL();
+  auto it = g_rt->textures.find(th);
+  if (it == g_rt->textures.end()) return fail(HSR_ERR_BAD_HANDLE, "texture_release: unknown texture");
+  cudaStreamSynchronize(g_rt->stream);
+  delete it->second;
+  g_rt->textures.erase(it);
+  return HSR_OK;
+}
+
+int hsr_target_create(int32_t w, int32_t h, hsr_target* out) {
+  RT_OR_FAIL();
+  if (!out || w <= 0 || h <= 0 || w > 32768 || h > 32768)
+    return fail(HSR_ERR_INVALID_ARG, "target: size must be in [1, 32768]");
+  TargetObj* t = new TargetObj();
+  t->w = w; t->h = h;
+  const size_t n = (size_t)w * (size_t)h;
+  int rc = dalloc((void**)&t->color, 4 * n, "target colour");
+  if (rc == HSR_OK) rc = dalloc((void**)&t->depth, 4 * n, "target depth");
+  if (rc == HSR_OK) rc = dalloc((void**)&t->prim, 4 * n, "target prim ids");
+  if (rc != HSR_OK) { delete t; return rc; }
+  // RenderBuffer's constructor clears to colour (0,0,0,1) -> bytes (0,0,0,255) and depth 1
+  // (renderbuffer.cpp:3-18)
+  const uint8_t rgba[4] = {0, 0, 0, 255};
+  const uint64_t hd = g_rt->next_handle++;
+  g_rt->targets[hd] = t;
+  *out = hd;
+  return g_rt->clear_target(t, rgba, 1.0f);
+}
+
+int hsr_target_release(hsr_target th) {
+  RT_OR_FAIL();
+  auto it = g_rt->targets.find(th);
+  if (it == g_rt->targets.end()) return fail(HSR_ERR_BAD_HANDLE, "target_release: unknown target");
+  cudaStreamSynchronize(g_rt->stream);
+  delete it->second;
+  g_rt->targets.erase(it);
+  return HSR_OK;
+}
+
+int hsr_target_clear(hsr_target th, const uint8_t rgba[4], float depth) {
+  RT_OR_FAIL();
+  TargetObj* t = g_rt->target(th);
+  if (!t) return fail(HSR_ERR_BAD_HANDLE, "target_clear: unknown target");
+  if (!rgba) return fail(HSR_ERR_INVALID_ARG, "target_clear: rgba is null");
+  return g_rt->clear_target(t, rgba, depth);
+}
+
+int hsr_target_upload(hsr_target th, const uint8_t* rgba, const float* depth, const uint32_t* prim) {
+  RT_OR_FAIL();
+  TargetObj* t = g_rt->target(th);
+  if (!t) return fail(HSR_ERR_BAD_HANDLE, "target_upload: unknown target");
+  const size_t n = (size_t)t->w * (size_t)t->h;
+  cudaError_t e = cudaSuccess;
+  if (rgba && e == cudaSuccess) e = cudaMemcpyAsync(t->color, rgba, 4 * n, cudaMemcpyHostToDevice, g_rt->stream);
+  if (depth && e == cudaSuccess) e = cudaMemcpyAsync(t->depth, depth, 4 * n, cudaMemcpyHostToDevice, g_rt->stream);
+  if (prim && e == cudaSuccess) e = cudaMemcpyAsync(t->prim, prim, 4 * n, cudaMemcpyHostToDevice, g_rt->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(g_rt->stream);
+  return e == cudaSuccess ? HSR_OK : cuda_fail(e, "target upload");
+}
+
+int hsr_target_download(hsr_target th, uint8_t* rgba, float* depth, uint32_t* prim) {
+  RT_OR_FAIL();
+  TargetObj* t = g_rt->target(th);
+  if (!t) return fail(HSR_ERR_BAD_HANDLE, "target_download: unknown target");
+  const size_t n = (size_t)t->w * (size_t)t->h;
+  cudaError_t e = cudaSuccess;
+  if (rgba && e == cudaSuccess) e = cudaMemcpyAsync(rgba, t->color, 4 * n, cudaMemcpyDeviceToHost, g_rt->stream);
+  if (depth && e == cudaSuccess) e = cudaMemcpyAsync(depth, t->depth, 4 * n, cudaMemcpyDeviceToHost, g_rt->stream);
+  if (prim && e == cudaSuccess) e = cudaMemcpyAsync(prim, t->prim, 4 * n, cudaMemcpyDeviceToHost, g_rt->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(g_rt->stream);
+  return e == cudaSuccess ? HSR_OK : cuda_fail(e, "target download");
+}
+
+int hsr_draw(const hsr_draw_desc* desc) {
+  RT_OR_FAIL();
+  if (!desc) return fail(HSR_ERR_INVALID_ARG, "draw: desc is null");
+  return g_rt->run_batch(desc, 1);
+}
+
+int hsr_draw_batch(const hsr_draw_desc* descs, int32_t n) {
+  RT_OR_FAIL();
+  if (n < 0 || (n > 0 && !descs)) return fail(HSR_ERR_INVALID_ARG, "draw_batch: bad arguments");
+  return g_rt->run_batch(descs, n);
+}
+
+int hsr_synchronize(void) {
+  RT_OR_FAIL();
+  cudaError_t e = cudaStreamSynchronize(g_rt->stream);
+  return e == cudaSuccess ? HSR_OK : cuda_fail(e, "synchronize");
+}
+
+int hsr_get_tuning(hsr_tuning* out) {
+  RT_OR_FAIL();
+  if (!out) return fail(HSR_ERR_INVALID_ARG, "get_tuning: null");
+  *out = g_rt->tuning;
+  return HSR_OK;
+}
+
+int hsr_set_tuning(const hsr_tuning* in) {
+  RT_OR_FAIL();
+  if (!in) return fail(HSR_ERR_INVALID_ARG, "set_tuning: null");
+  if (in->tile != 8 && in->tile != 16 && in->tile != 32) return fail(HSR_ERR_INVALID_ARG, "set_tuning: tile must be 8, 16 or 32");
+  if (in->warps_per_cta != 4 && in->warps_per_cta != 8) return fail(HSR_ERR_INVALID_ARG, "set_tuning: warps_per_cta must be 4 or 8");
+  if (in->tile == 32 && in->warps_per_cta != 4) return fail(HSR_ERR_INVALID_ARG, "set_tuning: tile 32 needs 4 warps per CTA");
+  if (in->ctas_per_sm < 1 || in->ctas_per_sm > 16) return fail(HSR_ERR_INVALID_ARG, "set_tuning: ctas_per_sm in [1,16]");
+  if (!(in->bin_factor >= 0.5f && in->bin_factor <= 64.f)) return fail(HSR_ERR_INVALID_ARG, "set_tuning: bin_factor in [0.5,64]");
+  g_rt->tuning = *in;
+  return HSR_OK;
+}
+
+int hsr_get_stats(hsr_stats* out) {
+  RT_OR_FAIL();
+  if (!out) return fail(HSR_ERR_INVALID_ARG, "get_stats: null");
+  *out = g_rt->stats;
+  out->kernel_launches = g_rt->launches;
+  return HSR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,86 @@
+// hsr_runtime.h — host-side objects behind the C ABI handles.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "hsr_internal.h"
+
+namespace hsr {
+
+struct MeshObj {  // Model (model.h:8-33) resident on the device
+  float *px = nullptr, *py = nullptr, *pz = nullptr;
+  float *nx = nullptr, *ny = nullptr, *nz = nullptr;
+  float2* uv = nullptr;
+  int4 *fv = nullptr, *fvt = nullptr, *fvn = nullptr;
+  int32_t npos = 0, nnrm = 0, nuv = 0, nfaces = 0;
+  ~MeshObj();
+};
+
+struct TexObj {  // TGAImage (tgaimage.h:66-98) as 32-bit BGRA words
+  uint32_t* words = nullptr;
+  int32_t w = 0, h = 0, bpp = 0;
+  ~TexObj();
+};
+
+struct TargetObj {  // RenderBuffer (renderbuffer.h:5-22) + prim-id plane
+  uint32_t* color = nullptr;  // RGBA8, byte order r, g, b, a
+  float* depth = nullptr;
+  uint32_t* prim = nullptr;
+  int32_t w = 0, h = 0;
+  ~TargetObj();
+};
+
+struct Arena {  // grow-only device scratch
+  char* base = nullptr;
+  size_t cap = 0;
+  int reserve(size_t bytes);
+};
+
+struct Pinned {  // grow-only pinned host staging
+  char* base = nullptr;
+  size_t cap = 0;
+  int reserve(size_t bytes);
+};
+
+struct Runtime {
+  int device = 0;
+  int num_sms = 1;
+  cudaStream_t stream = nullptr;
+  uint64_t next_handle = 1;
+  std::unordered_map<uint64_t, MeshObj*> meshes;
+  std::unordered_map<uint64_t, TexObj*> textures;
+  std::unordered_map<uint64_t, TargetObj*> targets;
+  Arena arena;
+  Pinned staging;
+  hsr_tuning tuning = {8, 4, 8, 4.0f};
+  hsr_stats stats = {};
+  uint64_t launches = 0;
+  size_t cap_rec_hint = 0, cap_clip_hint = 0, cap_bin_hint = 0;
+
+  MeshObj* mesh(uint64_t h);
+  TexObj* tex(uint64_t h);
+  TargetObj* target(uint64_t h);
+  int validate(const hsr_draw_desc& d);
+  int plan_order(const hsr_draw_desc* d, int n, std::vector<int>& order, std::vector<int>& dep0,
+                 std::vector<int>& dep1);
+  int run_batch(const hsr_draw_desc* descs, int n);
+  int clear_target(TargetObj* t, const uint8_t rgba[4], float depth);
+
+ private:
+  template <class T> T* get(std::unordered_map<uint64_t, T*>& m, uint64_t h);
+};
+
+extern Runtime* g_rt;
+extern std::mutex g_mu;
+extern thread_local std::string g_last_error;
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* where);
+void mat_mul_ref(const float* a, const float* b, float* out);
+int launch_clear(uint32_t* color, float* depth, uint32_t* prim, size_t n, uint32_t rgba, float d, cudaStream_t s);
+
+}  // namespace hsr

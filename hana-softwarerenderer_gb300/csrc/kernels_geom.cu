@@ -1,0 +1,314 @@
+// kernels_geom.cu — vertex transform and triangle setup (sm_103a).
+//
+// k_vertex replaces the per-corner IShader::vertex calls of graphics.cpp:380-387.  The
+// vertex shader is a pure function of its a2v inputs, and each output stream depends on
+// one attribute stream only (clip and world position on `v`, world normal and light
+// intensity on `vn`, uv passes through), so each attribute is transformed once and the
+// setup kernel gathers per corner: the same bits as three vertex() calls per face.
+//
+// k_setup follows graphics.cpp:136-161 (clip) and :314-347 (divide, cull, viewport,
+// bounding box) for every fan triangle and emits one RasterRec.  Faces that fail the fast
+// accept are clipped by the whole warp: lane k carries varying k of the polygon through
+// Sutherland-Hodgman while every lane evaluates the plane tests on the clip coordinates.
+#include <float.h>
+
+#include "hsr_device.cuh"
+
+namespace hsr {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// ---------------------------------------------------------------------------------------
+// vertex stage
+// ---------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_vertex(const DView* __restrict__ views, const Chunk* __restrict__ chunks) {
+  const Chunk ch = chunks[blockIdx.x];
+  const DView& v = views[ch.view];
+  const int i4 = ch.begin + (int)threadIdx.x * 4;
+  if (i4 >= ch.end) return;
+  if (ch.kind == 0) {
+    // positions: ObjectToClipPos / ObjectToViewPos (IShader.h:55-61), ObjectToWorldPos (:63-65)
+    const float4 X = __ldg(reinterpret_cast<const float4*>(v.px + i4));
+    const float4 Y = __ldg(reinterpret_cast<const float4*>(v.py + i4));
+    const float4 Z = __ldg(reinterpret_cast<const float4*>(v.pz + i4));
+    const float xs[4] = {X.x, X.y, X.z, X.w}, ys[4] = {Y.x, Y.y, Y.z, Y.w}, zs[4] = {Z.x, Z.y, Z.z, Z.w};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      if (i4 + k >= ch.end) break;
+      v.clip[i4 + k] = mat_vec(v.mvp, xs[k], ys[k], zs[k], 1.f);
+      if (v.wpos) {
+        float4 w = mat_vec(v.u.model_matrix, xs[k], ys[k], zs[k], 1.f);
+        v.wpos[i4 + k] = make_float4(w.x, w.y, w.z, 0.f);
+      }
+    }
+  } else {
+    // normals: ObjectToWorldNormal (IShader.h:71-75) = [n, 1] * model_I; intensity of
+    // Ground/Toon = saturate(worldN . light_dir) (IShader.cpp:8, :26)
+    const float4 X = __ldg(reinterpret_cast<const float4*>(v.nx + i4));
+    const float4 Y = __ldg(reinterpret_cast<const float4*>(v.ny + i4));
+    const float4 Z = __ldg(reinterpret_cast<const float4*>(v.nz + i4));
+    const float xs[4] = {X.x, X.y, X.z, X.w}, ys[4] = {Y.x, Y.y, Y.z, Y.w}, zs[4] = {Z.x, Z.y, Z.z, Z.w};
+    const float* m = v.u.model_matrix_I;
+    const F3 L = {v.u.light_dir[0], v.u.light_dir[1], v.u.light_dir[2]};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      if (i4 + k >= ch.end) break;
+      F3 wn;
+      wn.x = dot4(xs[k], ys[k], zs[k], 1.f, m[0], m[4], m[8], m[12]);
+      wn.y = dot4(xs[k], ys[k], zs[k], 1.f, m[1], m[5], m[9], m[13]);
+      wn.z = dot4(xs[k], ys[k], zs[k], 1.f, m[2], m[6], m[10], m[14]);
+      v.wnrm[i4 + k] = make_float4(wn.x, wn.y, wn.z, saturate(dot3(wn, L)));
+    }
+  }
+}
+
+int launch_vertex(const DView* views, const Chunk* chunks, int nchunks, cudaStream_t s) {
+  if (nchunks <= 0) return 0;
+  k_vertex<<<nchunks, 256, 0, s>>>(views, chunks);
+  return (int)cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------
+// setup stage
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ bool coord_ok(float c) {
+  float a = fabsf(c);
+  return (a == 0.f) || (a >= 0x1p-8f && a <= 0x1p20f);
+}
+
+// Divide, cull, viewport, bounding box of one fan triangle (graphics.cpp:314-347).
+__device__ __forceinline__ bool build_rec(const DView& v, float4 c0, float4 c1, float4 c2, uint32_t seq,
+                                          uint32_t view, RasterRec& r) {
+  const F3 n0 = {fd(c0.x, c0.w), fd(c0.y, c0.w), fd(c0.z, c0.w)};
+  const F3 n1 = {fd(c1.x, c1.w), fd(c1.y, c1.w), fd(c1.z, c1.w)};
+  const F3 n2 = {fd(c2.x, c2.w), fd(c2.y, c2.w), fd(c2.z, c2.w)};
+  // is_back_facing (:172-180), evaluated left to right
+  float sa = fs(fm(n0.x, n1.y), fm(n0.y, n1.x));
+  sa = fa(sa, fm(n1.x, n2.y));
+  sa = fs(sa, fm(n1.y, n2.x));
+  sa = fa(sa, fm(n2.x, n0.y));
+  sa = fs(sa, fm(n2.y, n0.x));
+  if (sa <= 0.f) return false;
+  const F3 s0 = viewport(v.W, v.H, n0), s1 = viewport(v.W, v.H, n1), s2 = viewport(v.W, v.H, n2);
+  // bounding box with std::min / std::max (:339-347)
+  float bminx = FLT_MAX, bminy = FLT_MAX, bmaxx = -FLT_MAX, bmaxy = -FLT_MAX;
+  const float clampx = (float)(v.W - 1), clampy = (float)(v.H - 1);
+  const float sx[3] = {s0.x, s1.x, s2.x}, sy[3] = {s0.y, s1.y, s2.y};
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    bminx = std_max(0.f, std_min(bminx, sx[i]));
+    bmaxx = std_min(clampx, std_max(bmaxx, sx[i]));
+    bminy = std_max(0.f, std_min(bminy, sy[i]));
+    bmaxy = std_min(clampy, std_max(bmaxy, sy[i]));
+  }
+  // pixels visited: x from (int)bboxmin.x while x <= bboxmax.x (:350-351)
+  const int32_t x0 = cvt_i32(bminx), y0 = cvt_i32(bminy);
+  if (x0 < 0 || y0 < 0 || bmaxx < 0.f || bmaxy < 0.f) return false;
+  const int32_t x1 = (int32_t)floorf(bmaxx), y1 = (int32_t)floorf(bmaxy);
+  if (x0 > x1 || y0 > y1) return false;
+  // barycentric() constants (:222-233): u.z = (C.x-A.x)(B.y-A.y) - (B.x-A.x)(C.y-A.y)
+  const float e1x = fs(s1.x, s0.x), e1y = fs(s1.y, s0.y);
+  const float e2x = fs(s2.x, s0.x), e2y = fs(s2.y, s0.y);
+  const float uz = fs(fm(e2x, e1y), fm(e1x, e2y));
+  if (!(fabsf(uz) > 0.01f)) return false;  // degenerate: every pixel gets (-1,1,1)
+  r.ax = s0.x; r.ay = s0.y; r.e1x = e1x; r.e1y = e1y;
+  r.e2x = e2x; r.e2y = e2y; r.uz = uz; r.d0 = s0.z;
+  r.d1 = s1.z; r.d2 = s2.z;
+  r.seq = seq; r.view = view;
+  r.xr = (uint32_t)x0 | ((uint32_t)x1 << 16);
+  r.yr = (uint32_t)y0 | ((uint32_t)y1 << 16);
+  const bool ok = coord_ok(s0.x) && coord_ok(s0.y) && coord_ok(s1.x) && coord_ok(s1.y) &&
+                  coord_ok(s2.x) && coord_ok(s2.y) && fabsf(uz) <= 0x1p30f;
+  r.flags = ok ? 0u : kRecExact;
+  r.pad = 0u;
+  return true;
+}
+
+__device__ __forceinline__ void store_rec(RasterRec* dst, const RasterRec& r) {
+  float4* d = reinterpret_cast<float4*>(dst);
+  const float4* s = reinterpret_cast<const float4*>(&r);
+  d[0] = s[0]; d[1] = s[1]; d[2] = s[2]; d[3] = s[3];
+}
+
+// Append the valid records of a warp and count the tiles each one touches.  All 32 lanes
+// of the warp must call this.
+__device__ void commit(bool valid, const RasterRec& r, const DView& v, int T, const Scratch& sc) {
+  const int lane = threadIdx.x & 31;
+  const unsigned m = __ballot_sync(kFull, valid);
+  if (!m) return;
+  const int leader = __ffs(m) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(&sc.ctl->rec_count, (uint32_t)__popc(m));
+  base = __shfl_sync(kFull, base, leader);
+  const uint32_t slot = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+  bool ok = valid && slot < sc.rec_cap;
+  if (valid && !ok) atomicOr(&sc.ctl->error, kErrRecOverflow);
+  if (ok) store_rec(&sc.recs[slot], r);
+
+  int tx0 = 0, ty0 = 0, ntw = 0, nt = 0;
+  if (ok) {
+    const int x0 = (int)(r.xr & 0xffffu), x1 = (int)(r.xr >> 16);
+    const int y0 = (int)(r.yr & 0xffffu), y1 = (int)(r.yr >> 16);
+    tx0 = x0 / T; ty0 = y0 / T;
+    ntw = x1 / T - tx0 + 1;
+    nt = ntw * (y1 / T - ty0 + 1);
+  }
+  const bool big = nt > kBigRecordTiles;
+  const int my_n = big ? 0 : nt;
+  const int maxn = __reduce_max_sync(kFull, my_n);
+  for (int k = 0; k < maxn; k++) {
+    const int tile = (k < my_n) ? v.tile_base + (ty0 + k / ntw) * v.tiles_x + tx0 + k % ntw : -1;
+    const unsigned grp = __match_any_sync(kFull, tile);
+    if (tile >= 0 && lane == __ffs(grp) - 1) atomicAdd(&sc.tile_count[tile], (uint32_t)__popc(grp));
+  }
+  unsigned bm = __ballot_sync(kFull, big);
+  while (bm) {
+    const int l = __ffs(bm) - 1;
+    bm &= bm - 1;
+    const int btx0 = __shfl_sync(kFull, tx0, l), bty0 = __shfl_sync(kFull, ty0, l);
+    const int bntw = __shfl_sync(kFull, ntw, l), bnt = __shfl_sync(kFull, nt, l);
+    for (int k = lane; k < bnt; k += 32)
+      atomicAdd(&sc.tile_count[v.tile_base + (bty0 + k / bntw) * v.tiles_x + btx0 + k % bntw], 1u);
+  }
+}
+
+enum { PW, PX, NX, PY, NY, PZ, NZ };
+
+// is_inside_plane (graphics.cpp:29-49) on clip coordinates c[0..3]
+__device__ __forceinline__ bool inside_plane(const float* c, int plane) {
+  switch (plane) {
+    case PW: return c[3] >= 1e-5f;
+    case PX: return c[0] <= c[3];
+    case NX: return c[0] >= -c[3];
+    case PY: return c[1] <= c[3];
+    case NY: return c[1] >= -c[3];
+    case PZ: return c[2] <= c[3];
+    default: return c[2] >= -c[3];
+  }
+}
+// get_intersect_ratio (graphics.cpp:51-71)
+__device__ __forceinline__ float intersect_ratio(const float* p, const float* q, int plane) {
+  switch (plane) {
+    case PW: return fd(fs(p[3], 1e-5f), fs(p[3], q[3]));
+    case PX: return fd(fs(p[3], p[0]), fs(fs(p[3], p[0]), fs(q[3], q[0])));
+    case NX: return fd(fa(p[3], p[0]), fs(fa(p[3], p[0]), fa(q[3], q[0])));
+    case PY: return fd(fs(p[3], p[1]), fs(fs(p[3], p[1]), fs(q[3], q[1])));
+    case NY: return fd(fa(p[3], p[1]), fs(fa(p[3], p[1]), fa(q[3], q[1])));
+    case PZ: return fd(fs(p[3], p[2]), fs(fs(p[3], p[2]), fs(q[3], q[2])));
+    default: return fd(fa(p[3], p[2]), fs(fa(p[3], p[2]), fa(q[3], q[2])));
+  }
+}
+__device__ __forceinline__ bool vertex_visible(float4 c) {  // is_vertex_visible (:132-134)
+  return fabsf(c.x) <= c.w && fabsf(c.y) <= c.w && fabsf(c.z) <= c.w;
+}
+
+constexpr int kSetupThreads = 256;
+constexpr int kPolyStride = kVaryings;  // floats per polygon vertex in shared memory
+
+__global__ void __launch_bounds__(kSetupThreads) k_setup(const DView* __restrict__ views,
+                                                         const Chunk* __restrict__ chunks, int T, Scratch sc) {
+  // per warp: two ping-pong polygons of up to 16 vertices x 13 varyings
+  __shared__ float poly[kSetupThreads / 32][2][16 * kPolyStride];
+  const Chunk ch = chunks[blockIdx.x];
+  const DView& v = views[ch.view];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int f = ch.begin + (int)threadIdx.x;
+  const bool active = f < ch.end;
+
+  // ---- fast accept (graphics.cpp:140-148) ---------------------------------------------
+  bool needs_clip = false, valid = false;
+  RasterRec r;
+  if (active) {
+    const int4 iv = __ldg(&v.fv[f]);
+    const float4 c0 = v.clip[iv.x], c1 = v.clip[iv.y], c2 = v.clip[iv.z];
+    if (vertex_visible(c0) && vertex_visible(c1) && vertex_visible(c2))
+      valid = build_rec(v, c0, c1, c2, (uint32_t)f << 4, (uint32_t)ch.view, r);
+    else
+      needs_clip = true;
+  }
+  commit(valid, r, v, T, sc);
+
+  // ---- homogeneous clipping, one face at a time per warp (graphics.cpp:73-161) ---------
+  unsigned cm = __ballot_sync(kFull, needs_clip);
+  while (cm) {
+    const int l = __ffs(cm) - 1;
+    cm &= cm - 1;
+    const int face = __shfl_sync(kFull, f, l);
+    float* A = poly[warp][0];
+    float* B = poly[warp][1];
+    if (lane < 3) {
+      const int4 iv = __ldg(&v.fv[face]), it = __ldg(&v.fvt[face]), in = __ldg(&v.fvn[face]);
+      const int pi = lane == 0 ? iv.x : (lane == 1 ? iv.y : iv.z);
+      const int ti = lane == 0 ? it.x : (lane == 1 ? it.y : it.z);
+      const int ni = lane == 0 ? in.x : (lane == 1 ? in.y : in.z);
+      float* o = A + lane * kPolyStride;
+      const float4 c = v.clip[pi];
+      o[0] = c.x; o[1] = c.y; o[2] = c.z; o[3] = c.w;
+      float4 wp = v.wpos ? v.wpos[pi] : make_float4(0.f, 0.f, 0.f, 0.f);
+      float4 wn = v.wnrm ? v.wnrm[ni] : make_float4(0.f, 0.f, 0.f, 0.f);
+      float2 t = v.uv ? __ldg(&v.uv[ti]) : make_float2(0.f, 0.f);
+      o[4] = wp.x; o[5] = wp.y; o[6] = wp.z;
+      o[7] = wn.x; o[8] = wn.y; o[9] = wn.z;
+      o[10] = t.x; o[11] = t.y; o[12] = wn.w;
+    }
+    __syncwarp();
+    int n = 3;
+    float* src = A;
+    float* dst = B;
+    for (int plane = PW; plane <= NZ && n >= 3; plane++) {
+      int m = 0;
+      for (int i = 0; i < n; i++) {
+        const float* prev = src + ((i - 1 + n) % n) * kPolyStride;
+        const float* curr = src + i * kPolyStride;
+        const bool pin = inside_plane(prev, plane), cin = inside_plane(curr, plane);
+        if (pin != cin) {
+          const float t = intersect_ratio(prev, curr, plane);
+          if (lane < kVaryings) dst[m * kPolyStride + lane] = fa(prev[lane], fm(fs(curr[lane], prev[lane]), t));
+          m++;
+        }
+        if (cin) {
+          if (lane < kVaryings) dst[m * kPolyStride + lane] = curr[lane];
+          m++;
+        }
+      }
+      __syncwarp();
+      n = m;
+      float* tmp = src; src = dst; dst = tmp;
+    }
+    bool cvalid = false;
+    RasterRec cr;
+    if (n >= 3) {
+      uint32_t slot = 0;
+      if (lane == 0) slot = atomicAdd(&sc.ctl->clip_count, 1u);
+      slot = __shfl_sync(kFull, slot, 0);
+      if (slot < sc.clip_cap) {
+        float* out = sc.clipbuf + (size_t)slot * kClipSlotFloats;
+        if (lane == 0) {
+          out[0] = __int_as_float(n);
+          v.clip_slot[face] = (int32_t)slot;
+        }
+        for (int k = lane; k < n * kVaryings; k += 32) out[4 + k] = src[k];
+        if (lane < n - 2) {
+          const float* p0 = src;
+          const float* p1 = src + (lane + 1) * kPolyStride;
+          const float* p2 = src + (lane + 2) * kPolyStride;
+          cvalid = build_rec(v, make_float4(p0[0], p0[1], p0[2], p0[3]), make_float4(p1[0], p1[1], p1[2], p1[3]),
+                             make_float4(p2[0], p2[1], p2[2], p2[3]),
+                             ((uint32_t)face << 4) | ((uint32_t)lane << 1) | 1u, (uint32_t)ch.view, cr);
+        }
+      } else if (lane == 0) {
+        atomicOr(&sc.ctl->error, kErrClipOverflow);
+      }
+    }
+    commit(cvalid, cr, v, T, sc);
+    __syncwarp();
+  }
+}
+
+int launch_setup(const DView* views, const Chunk* chunks, int nchunks, int tile, Scratch sc, cudaStream_t s) {
+  if (nchunks <= 0) return 0;
+  k_setup<<<nchunks, kSetupThreads, 0, s>>>(views, chunks, tile, sc);
+  return (int)cudaGetLastError();
+}
+
+}  // namespace hsr

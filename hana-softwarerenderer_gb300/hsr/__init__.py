@@ -1,0 +1,260 @@
+"""ctypes binding of libhsr.so, the GB300 draw path behind the C ABI in include/hsr.h.
+
+The library is the product; this module only marshals numpy arrays into its entry points.
+It never renders on the CPU: if libhsr.so is missing or no CUDA device is present, the
+calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .uniforms import SHADER_DATA_DTYPE  # noqa: F401  (re-exported)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(os.path.dirname(HERE), "lib", "libhsr.so")
+
+# status codes (include/hsr.h)
+OK, ERR_INVALID_ARG, ERR_UNKNOWN_SHADER, ERR_BIN_OVERFLOW, ERR_OUT_OF_MEMORY, ERR_TIMEOUT, ERR_CUDA, \
+    ERR_NOT_INITIALIZED, ERR_BAD_HANDLE, ERR_BUSY = range(10)
+DRAW_CLEAR = 1
+
+_u8p = ctypes.POINTER(ctypes.c_uint8)
+_f32p = ctypes.POINTER(ctypes.c_float)
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+
+
+class HsrError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"hsr error {code}: {msg}")
+        self.code = code
+
+
+class DrawDesc(ctypes.Structure):
+    _fields_ = [("mesh", ctypes.c_uint64), ("shader", ctypes.c_int32), ("flags", ctypes.c_uint32),
+                ("diffuse", ctypes.c_uint64), ("normal", ctypes.c_uint64), ("target", ctypes.c_uint64),
+                ("shadow_map", ctypes.c_uint64), ("uniforms", ctypes.c_void_p), ("prim_base", ctypes.c_uint32),
+                ("clear_depth", ctypes.c_float), ("clear_rgba", ctypes.c_uint8 * 4)]
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("tile", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("warps_per_cta", ctypes.c_int32),
+                ("bin_factor", ctypes.c_float)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("records", ctypes.c_uint64), ("clipped_faces", ctypes.c_uint64), ("bin_pairs", ctypes.c_uint64),
+                ("tiles", ctypes.c_uint64), ("retries", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64)]
+
+
+_lib = None
+
+
+def lib_path() -> str:
+    return LIB_PATH
+
+
+def lib():
+    """Load libhsr.so (built in-tree by build_lib.py); raise if it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with __graft_entry__.build()")
+    L = ctypes.CDLL(LIB_PATH)
+    sig = {
+        "hsr_init": ([ctypes.c_int], ctypes.c_int),
+        "hsr_shutdown": ([], ctypes.c_int),
+        "hsr_last_error": ([], ctypes.c_char_p),
+        "hsr_abi_version": ([], ctypes.c_int),
+        "hsr_mesh_upload": ([_f32p, ctypes.c_int32, _f32p, ctypes.c_int32, _f32p, ctypes.c_int32, _i32p,
+                             ctypes.c_int32, _u64p], ctypes.c_int),
+        "hsr_mesh_update_normals": ([ctypes.c_uint64, _f32p, ctypes.c_int32], ctypes.c_int),
+        "hsr_mesh_release": ([ctypes.c_uint64], ctypes.c_int),
+        "hsr_texture_upload": ([_u8p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _u64p], ctypes.c_int),
+        "hsr_texture_release": ([ctypes.c_uint64], ctypes.c_int),
+        "hsr_target_create": ([ctypes.c_int32, ctypes.c_int32, _u64p], ctypes.c_int),
+        "hsr_target_release": ([ctypes.c_uint64], ctypes.c_int),
+        "hsr_target_clear": ([ctypes.c_uint64, _u8p, ctypes.c_float], ctypes.c_int),
+        "hsr_target_upload": ([ctypes.c_uint64, _u8p, _f32p, _u32p], ctypes.c_int),
+        "hsr_target_download": ([ctypes.c_uint64, _u8p, _f32p, _u32p], ctypes.c_int),
+        "hsr_draw": ([ctypes.POINTER(DrawDesc)], ctypes.c_int),
+        "hsr_draw_batch": ([ctypes.POINTER(DrawDesc), ctypes.c_int32], ctypes.c_int),
+        "hsr_synchronize": ([], ctypes.c_int),
+        "hsr_get_tuning": ([ctypes.POINTER(Tuning)], ctypes.c_int),
+        "hsr_set_tuning": ([ctypes.POINTER(Tuning)], ctypes.c_int),
+        "hsr_get_stats": ([ctypes.POINTER(Stats)], ctypes.c_int),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return L
+
+
+def check(rc: int) -> None:
+    if rc != OK:
+        raise HsrError(rc, lib().hsr_last_error().decode(errors="replace"))
+
+
+def init(device: int = 0) -> None:
+    check(lib().hsr_init(device))
+
+
+def shutdown() -> None:
+    check(lib().hsr_shutdown())
+
+
+def synchronize() -> None:
+    check(lib().hsr_synchronize())
+
+
+def get_tuning() -> Tuning:
+    t = Tuning()
+    check(lib().hsr_get_tuning(ctypes.byref(t)))
+    return t
+
+
+def set_tuning(tile=None, ctas_per_sm=None, warps_per_cta=None, bin_factor=None) -> None:
+    t = get_tuning()
+    if tile is not None:
+        t.tile = tile
+    if ctas_per_sm is not None:
+        t.ctas_per_sm = ctas_per_sm
+    if warps_per_cta is not None:
+        t.warps_per_cta = warps_per_cta
+    if bin_factor is not None:
+        t.bin_factor = bin_factor
+    check(lib().hsr_set_tuning(ctypes.byref(t)))
+
+
+def stats() -> dict:
+    s = Stats()
+    check(lib().hsr_get_stats(ctypes.byref(s)))
+    return {k: int(getattr(s, k)) for k, _ in Stats._fields_}
+
+
+class Mesh:
+    """A Model resident on the device (hsr_mesh_upload)."""
+
+    def __init__(self, mesh):
+        pos = np.ascontiguousarray(mesh.pos, np.float32)
+        nrm = np.ascontiguousarray(mesh.nrm, np.float32)
+        uv = np.ascontiguousarray(mesh.uv, np.float32)
+        faces = np.ascontiguousarray(mesh.faces, np.int32)
+        h = ctypes.c_uint64()
+        check(lib().hsr_mesh_upload(pos.ctypes.data_as(_f32p), len(pos), nrm.ctypes.data_as(_f32p), len(nrm),
+                                    uv.ctypes.data_as(_f32p), len(uv), faces.ctypes.data_as(_i32p), len(faces),
+                                    ctypes.byref(h)))
+        self.handle = h.value
+        self.nfaces = len(faces)
+
+    def update_normals(self, nrm: np.ndarray) -> None:
+        nrm = np.ascontiguousarray(nrm, np.float32)
+        check(lib().hsr_mesh_update_normals(self.handle, nrm.ctypes.data_as(_f32p), len(nrm)))
+
+    def release(self) -> None:
+        if self.handle:
+            check(lib().hsr_mesh_release(self.handle))
+            self.handle = 0
+
+
+class Texture:
+    """A TGAImage resident on the device (hsr_texture_upload)."""
+
+    def __init__(self, tex):
+        d = np.ascontiguousarray(tex.data, np.uint8)
+        h = ctypes.c_uint64()
+        check(lib().hsr_texture_upload(d.ctypes.data_as(_u8p), tex.w, tex.h, tex.bpp, ctypes.byref(h)))
+        self.handle = h.value
+
+    def release(self) -> None:
+        if self.handle:
+            check(lib().hsr_texture_release(self.handle))
+            self.handle = 0
+
+
+class Target:
+    """A RenderBuffer (+ prim-id plane) resident on the device."""
+
+    def __init__(self, w: int, h: int):
+        hd = ctypes.c_uint64()
+        check(lib().hsr_target_create(w, h, ctypes.byref(hd)))
+        self.handle = hd.value
+        self.w, self.h = w, h
+
+    def clear(self, rgba=(0, 0, 0, 1), depth=float(np.finfo(np.float32).max)) -> None:
+        c = (ctypes.c_uint8 * 4)(*rgba)
+        check(lib().hsr_target_clear(self.handle, ctypes.cast(c, _u8p), depth))
+
+    def upload(self, color=None, depth=None, prim=None) -> None:
+        c = None if color is None else np.ascontiguousarray(color, np.uint8)
+        d = None if depth is None else np.ascontiguousarray(depth, np.float32)
+        p = None if prim is None else np.ascontiguousarray(prim, np.uint32)
+        check(lib().hsr_target_upload(self.handle, c.ctypes.data_as(_u8p) if c is not None else None,
+                                      d.ctypes.data_as(_f32p) if d is not None else None,
+                                      p.ctypes.data_as(_u32p) if p is not None else None))
+
+    def download(self, color=True, depth=True, prim=True, out=None):
+        """Returns dict(color (h,w,4) u8, depth (h,w) f32, prim (h,w) u32); `out` may hold
+        preallocated (pinned or not) arrays to fill."""
+        out = out or {}
+        c = out.get("color") if color else None
+        d = out.get("depth") if depth else None
+        p = out.get("prim") if prim else None
+        if color and c is None:
+            c = np.empty((self.h, self.w, 4), np.uint8)
+        if depth and d is None:
+            d = np.empty((self.h, self.w), np.float32)
+        if prim and p is None:
+            p = np.empty((self.h, self.w), np.uint32)
+        check(lib().hsr_target_download(self.handle, c.ctypes.data_as(_u8p) if c is not None else None,
+                                        d.ctypes.data_as(_f32p) if d is not None else None,
+                                        p.ctypes.data_as(_u32p) if p is not None else None))
+        return {"color": c, "depth": d, "prim": p}
+
+    def release(self) -> None:
+        if self.handle:
+            check(lib().hsr_target_release(self.handle))
+            self.handle = 0
+
+
+def make_desc(mesh: Mesh, shader: int, sd: np.ndarray, target: Target, diffuse: Texture | None = None,
+              normal: Texture | None = None, shadow_map: Target | None = None, prim_base: int = 0,
+              clear=None, keep: list | None = None) -> DrawDesc:
+    """Fill an hsr_draw_desc.  `clear=(rgba, depth)` fuses the clear into the draw.  The
+    uniform record must stay alive until the draw call returns: it is appended to `keep`."""
+    sdb = np.ascontiguousarray(np.asarray(sd, dtype=SHADER_DATA_DTYPE).reshape(()))
+    if keep is not None:
+        keep.append(sdb)
+    d = DrawDesc()
+    d.mesh = mesh.handle
+    d.shader = shader
+    d.flags = DRAW_CLEAR if clear is not None else 0
+    d.diffuse = diffuse.handle if diffuse else 0
+    d.normal = normal.handle if normal else 0
+    d.target = target.handle
+    d.shadow_map = shadow_map.handle if shadow_map else 0
+    d.uniforms = sdb.ctypes.data
+    d.prim_base = prim_base
+    if clear is not None:
+        rgba, depth = clear
+        d.clear_depth = float(depth)
+        for i in range(4):
+            d.clear_rgba[i] = rgba[i]
+    d._keep = sdb  # noqa: SLF001  keep the uniforms alive with the struct
+    return d
+
+
+def draw(desc: DrawDesc) -> None:
+    check(lib().hsr_draw(ctypes.byref(desc)))
+
+
+def draw_batch(descs) -> None:
+    arr = (DrawDesc * len(descs))(*descs)
+    check(lib().hsr_draw_batch(arr, len(descs)))

@@ -28,6 +28,12 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#if defined(_WIN32)
+#define HSR_API __declspec(dllexport)
+#else
+#define HSR_API __attribute__((visibility("default")))
+#endif
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -107,10 +113,10 @@ typedef struct hsr_draw_desc {
 } hsr_draw_desc;
 
 /* ---- lifetime ----------------------------------------------------------------------- */
-int hsr_init(int device);                 /* select device, create stream and scratch   */
-int hsr_shutdown(void);                   /* release every handle and device memory     */
-const char* hsr_last_error(void);         /* text of the last failure on this thread    */
-int hsr_abi_version(void);
+HSR_API int hsr_init(int device);                 /* select device, create stream and scratch   */
+HSR_API int hsr_shutdown(void);                   /* release every handle and device memory     */
+HSR_API const char* hsr_last_error(void);         /* text of the last failure on this thread    */
+HSR_API int hsr_abi_version(void);
 
 /* ---- meshes: Model (model.h:8-33) --------------------------------------------------
  * pos [npos][3], nrm [nnrm][3], uv [nuv][2]; faces [nfaces][3 corners][3] holding the
@@ -118,38 +124,38 @@ int hsr_abi_version(void);
  * Indices are validated on the host.  Normals are used as stored: the reference
  * normalises them in place on every access (model.cpp:108-111), which is the identity
  * for normals that are fixed points of Vector3f::normalize(). */
-int hsr_mesh_upload(const float* pos, int32_t npos, const float* nrm, int32_t nnrm,
+HSR_API int hsr_mesh_upload(const float* pos, int32_t npos, const float* nrm, int32_t nnrm,
                     const float* uv, int32_t nuv, const int32_t* faces, int32_t nfaces,
                     hsr_mesh* out);
 /* Replace the normal array of a mesh (same count), e.g. per-corner normals a drop-in
  * shim extracted through Model::normal(). */
-int hsr_mesh_update_normals(hsr_mesh mesh, const float* nrm, int32_t nnrm);
-int hsr_mesh_release(hsr_mesh mesh);
+HSR_API int hsr_mesh_update_normals(hsr_mesh mesh, const float* nrm, int32_t nnrm);
+HSR_API int hsr_mesh_release(hsr_mesh mesh);
 
 /* ---- textures: TGAImage (tgaimage.h:66-98) ------------------------------------------
  * data is the TGAImage buffer: texel (x,y) at (x + y*w)*bytespp, bytes B,G,R(,A);
  * bytespp in {1,3,4}.  Sampling is TGAImage::get (tgaimage.cpp:248-253). */
-int hsr_texture_upload(const uint8_t* data, int32_t w, int32_t h, int32_t bytespp,
+HSR_API int hsr_texture_upload(const uint8_t* data, int32_t w, int32_t h, int32_t bytespp,
                        hsr_texture* out);
-int hsr_texture_release(hsr_texture tex);
+HSR_API int hsr_texture_release(hsr_texture tex);
 
 /* ---- render targets: RenderBuffer (renderbuffer.h:5-22) + a prim-id plane ------------ */
-int hsr_target_create(int32_t w, int32_t h, hsr_target* out);
-int hsr_target_release(hsr_target t);
-int hsr_target_clear(hsr_target t, const uint8_t rgba[4], float depth); /* prim ids -> 0 */
+HSR_API int hsr_target_create(int32_t w, int32_t h, hsr_target* out);
+HSR_API int hsr_target_release(hsr_target t);
+HSR_API int hsr_target_clear(hsr_target t, const uint8_t rgba[4], float depth); /* prim ids -> 0 */
 /* Copy host RenderBuffer contents in (color_buffer RGBA8, depth_buffer FP32); prim may be NULL. */
-int hsr_target_upload(hsr_target t, const uint8_t* rgba, const float* depth, const uint32_t* prim);
+HSR_API int hsr_target_upload(hsr_target t, const uint8_t* rgba, const float* depth, const uint32_t* prim);
 /* Copy out; any pointer may be NULL.  Synchronises with the draws queued before it. */
-int hsr_target_download(hsr_target t, uint8_t* rgba, float* depth, uint32_t* prim);
+HSR_API int hsr_target_download(hsr_target t, uint8_t* rgba, float* depth, uint32_t* prim);
 
 /* ---- drawing -------------------------------------------------------------------------
  * hsr_draw: one graphics_draw_triangle() call, queued on the library stream.
  * hsr_draw_batch: n draws in one launch sequence.  A draw whose shadow_map is the target
  * of another draw in the batch runs after it (the DrawModel::draw order, scene.h:86-91);
  * several draws into one target keep their array order. */
-int hsr_draw(const hsr_draw_desc* desc);
-int hsr_draw_batch(const hsr_draw_desc* descs, int32_t n);
-int hsr_synchronize(void);
+HSR_API int hsr_draw(const hsr_draw_desc* desc);
+HSR_API int hsr_draw_batch(const hsr_draw_desc* descs, int32_t n);
+HSR_API int hsr_synchronize(void);
 
 /* ---- tuning ------------------------------------------------------------------------- */
 typedef struct hsr_tuning {
@@ -158,8 +164,8 @@ typedef struct hsr_tuning {
   int32_t warps_per_cta;  /* warps per raster CTA (one warp owns one tile)          */
   float bin_factor;       /* bin capacity = bin_factor * (faces + tiles) pairs      */
 } hsr_tuning;
-int hsr_get_tuning(hsr_tuning* out);
-int hsr_set_tuning(const hsr_tuning* in);
+HSR_API int hsr_get_tuning(hsr_tuning* out);
+HSR_API int hsr_set_tuning(const hsr_tuning* in);
 
 /* ---- statistics of the last completed draw sequence (for tests and benchmarks) ------- */
 typedef struct hsr_stats {
@@ -170,7 +176,7 @@ typedef struct hsr_stats {
   uint64_t retries;       /* scratch re-sizes after an overflow                    */
   uint64_t kernel_launches; /* kernels this library launched since hsr_init         */
 } hsr_stats;
-int hsr_get_stats(hsr_stats* out);
+HSR_API int hsr_get_stats(hsr_stats* out);
 
 #ifdef __cplusplus
 }

@@ -97,8 +97,12 @@ def run(frame, shader: int | None = None, obj_mesh=None, workdir: str | None = N
 
 def run_prim_ids(frame) -> dict:
     """Reference coverage/depth plus prim ids (face id + 1, 0 = untouched) per pass."""
+    import dataclasses
+
     from hsr import scenes
 
+    # ids are >= 1, so a black clear marks untouched pixels as 0 (depth does not depend on it)
+    frame = dataclasses.replace(frame, clear_rgba=(0, 0, 0, 0), shadow_clear_rgba=(0, 0, 0, 0))
     res = run(frame, shader=8 if frame.shader == scenes.SHADOW else 7, obj_mesh=scenes.prim_id_mesh(frame.mesh))
     for v in res.values():
         c = v["color"].astype(np.uint32)

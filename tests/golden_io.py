@@ -1,0 +1,45 @@
+"""Load the golden fixtures written by tests/golden/make_golden.py."""
+from __future__ import annotations
+
+import glob
+import os
+
+import numpy as np
+
+from hsr import scenes, uniforms as U
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def names() -> list[str]:
+    return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+def load(name: str):
+    """Returns (frame, expected) where expected[pass] = {depth, color, prim}."""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    mesh = scenes.Mesh(z["pos"], z["nrm"], z["uv"], z["faces"])
+    sd = np.frombuffer(z["sd"].tobytes(), U.SHADER_DATA_DTYPE).reshape(())
+    fr = scenes.Frame(mesh, int(z["shader"]), sd, int(z["width"]), int(z["height"]),
+                      diffuse=scenes.Texture(z["diffuse"]) if "diffuse" in z else None,
+                      normal=scenes.Texture(z["normal"]) if "normal" in z else None,
+                      shadow_size=tuple(int(v) for v in z["shadow_size"]),
+                      clear_rgba=tuple(int(v) for v in z["clear_rgba"]), clear_depth=float(z["clear_depth"]),
+                      shadow_clear_rgba=tuple(int(v) for v in z["shadow_clear_rgba"]),
+                      shadow_clear_depth=float(z["shadow_clear_depth"]), name=str(z["name"]))
+    exp = {}
+    for k in ("main", "shadow"):
+        if f"{k}_depth" in z:
+            exp[k] = {"depth": z[f"{k}_depth"], "color": z[f"{k}_color"], "prim": z[f"{k}_prim"]}
+    return fr, exp
+
+
+def compare(got: dict, exp: dict, color_tol: int = 1) -> dict:
+    """Bit-exact depth and prim ids, colour RGB within `color_tol` LSB; returns a report."""
+    d_bad = int((got["depth"].view(np.uint32) != exp["depth"].view(np.uint32)).sum())
+    p_bad = int((got["prim"] != exp["prim"]).sum())
+    dc = np.abs(got["color"][..., :3].astype(np.int32) - exp["color"][..., :3].astype(np.int32))
+    a_bad = int((got["color"][..., 3] != exp["color"][..., 3]).sum())
+    return {"depth_mismatch": d_bad, "prim_mismatch": p_bad, "color_max_err": int(dc.max()) if dc.size else 0,
+            "color_diff_px": int((dc.max(axis=-1) > 0).sum()), "alpha_mismatch": a_bad,
+            "color_ok": bool(dc.max() <= color_tol) if dc.size else True}
