@@ -22,7 +22,9 @@ namespace hsr {
 constexpr int kMaxPoly = 10;              // 3 vertices + one per clip plane (7 planes)
 constexpr int kVaryings = 13;             // floats in shader_struct_v2f (IShader.h:41-47)
 constexpr int kClipSlotFloats = 4 + kMaxPoly * kVaryings + 2;  // n, pad[3], verts, pad -> 136
-constexpr int kBigRecordTiles = 32;       // records touching more tiles are binned by a warp
+constexpr int kMaxRecordTiles = 32;       // records never touch more tiles (big ones are split)
+constexpr int kSubTilesX = 8, kSubTilesY = 4;  // tile block of one sub-record
+constexpr int kPayloadFloats = 32;        // per-record shading payload (see Payload layout)
 
 // Error bits in Ctl::error.
 enum : uint32_t {
@@ -49,6 +51,16 @@ struct __align__(16) RasterRec {
   uint32_t view;            // index of the view in the batch
   uint32_t xr, yr;          // inclusive pixel range: x0 | x1 << 16, y0 | y1 << 16
   uint32_t flags, pad;
+};
+
+// Per-record shading payload (kPayloadFloats floats, same index as the record): the
+// reciprocal w of each corner (graphics.cpp:333-337) and the corner varyings the shader
+// reads, so that shading a pixel needs the record and this payload only.
+//   [0..2] 1/w of corners 0..2, [3] unused,
+//   corner k at 4 + 9k: world_pos[3], world_normal[3], uv[2], scalar
+//   (scalar = clip_pos.z for ShadowShader, intensity for Ground/Toon).
+struct __align__(16) Payload {
+  float f[kPayloadFloats];
 };
 static_assert(sizeof(RasterRec) == 64, "RasterRec must stay 64 bytes");
 
@@ -83,6 +95,7 @@ struct DView {
   uint32_t prim_base;
   float clear_depth;
   uint32_t clear_rgba;
+  int32_t has_dependents;  // another view of the batch waits for this one's tiles
 };
 
 struct Ctl {
@@ -94,6 +107,7 @@ struct Ctl {
   uint32_t bin_total;
   uint32_t raster_tiles;
   uint32_t pad;
+  unsigned long long shaded_px;  // pixels whose winner was shaded by the raster
 };
 
 // Work chunk for the vertex and setup kernels: items [begin, end) of one view.
@@ -109,6 +123,7 @@ struct Scratch {
   Ctl* ctl;
   uint32_t* view_done;      // [nviews] tiles finished per view
   RasterRec* recs;  uint32_t rec_cap;
+  Payload* pay;             // [rec_cap]
   float* clipbuf;   uint32_t clip_cap;   // kClipSlotFloats per slot
   uint32_t* tile_count;     // [ntiles]
   uint32_t* tile_fill;      // [ntiles]

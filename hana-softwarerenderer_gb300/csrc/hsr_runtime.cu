@@ -170,8 +170,7 @@ int Runtime::plan_order(const hsr_draw_desc* d, int n, std::vector<int>& order, 
   return HSR_OK;
 }
 
-int Runtime::run_batch(const hsr_draw_desc* descs, int n) {
-  if (n <= 0) return HSR_OK;
+int Runtime::plan_build(const hsr_draw_desc* descs, int n, Plan& p) {
   for (int i = 0; i < n; i++) {
     int rc = validate(descs[i]);
     if (rc != HSR_OK) return rc;
@@ -183,18 +182,18 @@ int Runtime::run_batch(const hsr_draw_desc* descs, int n) {
   for (int k = 0; k < n; k++) pos[order[k]] = k;
 
   const int T = tuning.tile;
-  // ---- host-side view descriptors and scratch layout --------------------------------
-  std::vector<DView> views(n);
-  std::vector<Chunk> vchunks, schunks;
-  size_t total_faces = 0, total_tiles = 0;
-  struct Off { size_t clip, wpos, wnrm, slot; };
-  std::vector<Off> offs(n);
+  p = Plan();
+  p.n = n;
+  p.tile = T;
+  p.views.resize(n);
+  p.offs.resize(n);
+  p.order = order;
   size_t bytes = 0;
   for (int k = 0; k < n; k++) {
     const hsr_draw_desc& d = descs[order[k]];
     MeshObj* m = mesh(d.mesh);
     TargetObj* tg = target(d.target);
-    DView& v = views[k];
+    DView& v = p.views[k];
     std::memset(&v, 0, sizeof(v));
     v.px = m->px; v.py = m->py; v.pz = m->pz;
     v.nx = m->nx; v.ny = m->ny; v.nz = m->nz;
@@ -223,120 +222,197 @@ int Runtime::run_batch(const hsr_draw_desc* descs, int n) {
     v.tiles_x = (tg->w + T - 1) / T;
     v.tiles_y = (tg->h + T - 1) / T;
     v.ntiles = v.tiles_x * v.tiles_y;
-    v.tile_base = (int32_t)total_tiles;
+    v.tile_base = (int32_t)p.total_tiles;
     v.prim_base = d.prim_base;
     v.clear_depth = d.clear_depth;
     std::memcpy(&v.clear_rgba, d.clear_rgba, 4);
-    total_tiles += (size_t)v.ntiles;
-    total_faces += (size_t)m->nfaces;
-    Off& o = offs[k];
+    p.total_tiles += (size_t)v.ntiles;
+    p.total_faces += (size_t)m->nfaces;
+    p.total_pos += (size_t)m->npos;
+    p.total_pixels += (size_t)tg->w * (size_t)tg->h;
+    Plan::Off& o = p.offs[k];
     o.clip = bytes; bytes = align_up(bytes + sizeof(float4) * (size_t)std::max(m->npos, 1), 256);
-    o.wpos = bytes; if (shader_needs_wpos(d.shader)) bytes = align_up(bytes + sizeof(float4) * (size_t)std::max(m->npos, 1), 256);
-    o.wnrm = bytes; if (shader_needs_wnrm(d.shader)) bytes = align_up(bytes + sizeof(float4) * (size_t)std::max(m->nnrm, 1), 256);
-    o.slot = bytes; bytes = align_up(bytes + sizeof(int32_t) * (size_t)std::max(m->nfaces, 1), 256);
-    for (int b = 0; b < m->npos; b += 1024) vchunks.push_back({k, 0, b, std::min(m->npos, b + 1024)});
-    if (shader_needs_wnrm(d.shader))
-      for (int b = 0; b < m->nnrm; b += 1024) vchunks.push_back({k, 1, b, std::min(m->nnrm, b + 1024)});
-    for (int b = 0; b < m->nfaces; b += 256) schunks.push_back({k, 0, b, std::min(m->nfaces, b + 256)});
-  }
-  if (total_tiles > (size_t)INT32_MAX) return fail(HSR_ERR_INVALID_ARG, "draw batch: too many tiles");
-  const size_t view_bytes = bytes;
-
-  // capacities (grow on overflow, remembered across calls)
-  size_t rec_cap = std::max<size_t>(cap_rec_hint, total_faces + total_faces / 4 + 1024);
-  size_t clip_cap = std::max<size_t>(cap_clip_hint, total_faces / 16 + 256);
-  size_t bin_cap = std::max<size_t>(cap_bin_hint, (size_t)(tuning.bin_factor * (double)(total_faces + total_tiles)) + 4096);
-
-  for (int attempt = 0; attempt < 6; attempt++) {
-    rec_cap = std::min<size_t>(rec_cap, 0xfffff000u);
-    clip_cap = std::min<size_t>(clip_cap, 0xfffff000u);
-    bin_cap = std::min<size_t>(bin_cap, 0xfffff000u);
-    const int nscan = scan_blocks((int)total_tiles);
-    // layout: [views | chunks | per-view vertex outputs | ctl | view_done | tile_count |
-    //          tile_fill | scan_status | tile_off | recs | clipbuf | bins]
-    size_t off = 0;
-    const size_t o_views = off; off = align_up(off + sizeof(DView) * n, 256);
-    const size_t o_vch = off; off = align_up(off + sizeof(Chunk) * std::max<size_t>(vchunks.size(), 1), 256);
-    const size_t o_sch = off; off = align_up(off + sizeof(Chunk) * std::max<size_t>(schunks.size(), 1), 256);
-    const size_t o_vout = off; off = align_up(off + view_bytes, 256);
-    const size_t o_zero = off;
-    const size_t o_ctl = off; off = align_up(off + sizeof(Ctl), 256);
-    const size_t o_done = off; off = align_up(off + sizeof(uint32_t) * n, 256);
-    const size_t o_cnt = off; off = align_up(off + sizeof(uint32_t) * total_tiles, 256);
-    const size_t o_fill = off; off = align_up(off + sizeof(uint32_t) * total_tiles, 256);
-    const size_t o_stat = off; off = align_up(off + sizeof(unsigned long long) * std::max(nscan, 1), 256);
-    const size_t zero_bytes = off - o_zero;
-    const size_t o_toff = off; off = align_up(off + sizeof(uint32_t) * total_tiles, 256);
-    const size_t o_recs = off; off = align_up(off + sizeof(RasterRec) * rec_cap, 256);
-    const size_t o_clip = off; off = align_up(off + sizeof(float) * kClipSlotFloats * clip_cap, 256);
-    const size_t o_bins = off; off = align_up(off + sizeof(uint32_t) * bin_cap, 256);
-    int rc2 = arena.reserve(off);
-    if (rc2 != HSR_OK) return rc2;
-    char* B = arena.base;
-    for (int k = 0; k < n; k++) {
-      DView& v = views[k];
-      v.clip = (float4*)(B + o_vout + offs[k].clip);
-      v.wpos = shader_needs_wpos(v.shader) ? (float4*)(B + o_vout + offs[k].wpos) : nullptr;
-      v.wnrm = shader_needs_wnrm(v.shader) ? (float4*)(B + o_vout + offs[k].wnrm) : nullptr;
-      v.clip_slot = (int32_t*)(B + o_vout + offs[k].slot);
+    o.wpos = bytes;
+    if (shader_needs_wpos(d.shader)) bytes = align_up(bytes + sizeof(float4) * (size_t)std::max(m->npos, 1), 256);
+    o.wnrm = bytes;
+    if (shader_needs_wnrm(d.shader)) {
+      bytes = align_up(bytes + sizeof(float4) * (size_t)std::max(m->nnrm, 1), 256);
+      p.total_nrm += (size_t)m->nnrm;
     }
-    const size_t host_bytes = o_vout;
-    rc2 = staging.reserve(host_bytes + sizeof(Ctl));
-    if (rc2 != HSR_OK) return rc2;
-    std::memcpy(staging.base + o_views, views.data(), sizeof(DView) * n);
-    if (!vchunks.empty()) std::memcpy(staging.base + o_vch, vchunks.data(), sizeof(Chunk) * vchunks.size());
-    if (!schunks.empty()) std::memcpy(staging.base + o_sch, schunks.data(), sizeof(Chunk) * schunks.size());
+    o.slot = bytes; bytes = align_up(bytes + sizeof(int32_t) * (size_t)std::max(m->nfaces, 1), 256);
+    for (int b = 0; b < m->npos; b += 1024) p.vchunks.push_back({k, 0, b, std::min(m->npos, b + 1024)});
+    if (shader_needs_wnrm(d.shader))
+      for (int b = 0; b < m->nnrm; b += 1024) p.vchunks.push_back({k, 1, b, std::min(m->nnrm, b + 1024)});
+    for (int b = 0; b < m->nfaces; b += 256) p.schunks.push_back({k, 0, b, std::min(m->nfaces, b + 256)});
+  }
+  for (int k = 0; k < n; k++) {
+    if (p.views[k].dep0 >= 0) p.views[p.views[k].dep0].has_dependents = 1;
+    if (p.views[k].dep1 >= 0) p.views[p.views[k].dep1].has_dependents = 1;
+  }
+  if (p.total_tiles > (size_t)INT32_MAX) return fail(HSR_ERR_INVALID_ARG, "draw batch: too many tiles");
+  p.view_bytes = bytes;
+  p.rec_cap = std::max<size_t>(cap_rec_hint, p.total_faces + p.total_faces / 4 + 1024);
+  p.clip_cap = std::max<size_t>(cap_clip_hint, p.total_faces / 16 + 256);
+  p.bin_cap = std::max<size_t>(cap_bin_hint,
+                               (size_t)(tuning.bin_factor * (double)(p.total_faces + p.total_tiles)) + 4096);
+  return HSR_OK;
+}
 
-    Scratch sc;
-    sc.ctl = (Ctl*)(B + o_ctl);
-    sc.view_done = (uint32_t*)(B + o_done);
-    sc.recs = (RasterRec*)(B + o_recs); sc.rec_cap = (uint32_t)rec_cap;
-    sc.clipbuf = (float*)(B + o_clip); sc.clip_cap = (uint32_t)clip_cap;
-    sc.tile_count = (uint32_t*)(B + o_cnt);
-    sc.tile_fill = (uint32_t*)(B + o_fill);
-    sc.tile_off = (uint32_t*)(B + o_toff);
-    sc.scan_status = (unsigned long long*)(B + o_stat);
-    sc.bins = (uint32_t*)(B + o_bins); sc.bin_cap = (uint32_t)bin_cap;
-    sc.ntiles = (int32_t)total_tiles;
-    sc.nviews = n;
+void Plan::layout() {
+  rec_cap = std::min<size_t>(rec_cap, 0xfffff000u);
+  clip_cap = std::min<size_t>(clip_cap, 0xfffff000u);
+  bin_cap = std::min<size_t>(bin_cap, 0xfffff000u);
+  nscan = scan_blocks((int)total_tiles);
+  // [views | chunks | per-view vertex outputs | ctl | view_done | tile_count | tile_fill |
+  //  scan_status | tile_off | recs | clipbuf | bins]; the zeroed part is one memset
+  size_t off = 0;
+  o_views = off; off = align_up(off + sizeof(DView) * n, 256);
+  o_vch = off; off = align_up(off + sizeof(Chunk) * std::max<size_t>(vchunks.size(), 1), 256);
+  o_sch = off; off = align_up(off + sizeof(Chunk) * std::max<size_t>(schunks.size(), 1), 256);
+  host_bytes = off;
+  o_vout = off; off = align_up(off + view_bytes, 256);
+  o_zero = off;
+  o_ctl = off; off = align_up(off + sizeof(Ctl), 256);
+  o_done = off; off = align_up(off + sizeof(uint32_t) * n, 256);
+  o_cnt = off; off = align_up(off + sizeof(uint32_t) * total_tiles, 256);
+  o_fill = off; off = align_up(off + sizeof(uint32_t) * total_tiles, 256);
+  o_stat = off; off = align_up(off + sizeof(unsigned long long) * std::max(nscan, 1), 256);
+  zero_bytes = off - o_zero;
+  o_toff = off; off = align_up(off + sizeof(uint32_t) * total_tiles, 256);
+  o_recs = off; off = align_up(off + sizeof(RasterRec) * rec_cap, 256);
+  o_pay = off; off = align_up(off + sizeof(Payload) * rec_cap, 256);
+  o_clip = off; off = align_up(off + sizeof(float) * kClipSlotFloats * clip_cap, 256);
+  o_bins = off; off = align_up(off + sizeof(uint32_t) * bin_cap, 256);
+  dev_bytes = off;
+  stage_bytes = host_bytes + sizeof(Ctl);
+}
 
-    const DView* dviews = (const DView*)(B + o_views);
-    cudaError_t e = cudaMemcpyAsync(B, staging.base, host_bytes, cudaMemcpyHostToDevice, stream);
-    if (e != cudaSuccess) return cuda_fail(e, "upload views");
-    e = cudaMemsetAsync(B + o_zero, 0, zero_bytes, stream);
-    if (e != cudaSuccess) return cuda_fail(e, "clear scratch");
-    int kr = launch_vertex(dviews, (const Chunk*)(B + o_vch), (int)vchunks.size(), stream);
-    if (kr) return cuda_fail((cudaError_t)kr, "vertex kernel");
-    kr = launch_setup(dviews, (const Chunk*)(B + o_sch), (int)schunks.size(), T, sc, stream);
-    if (kr) return cuda_fail((cudaError_t)kr, "setup kernel");
-    kr = launch_scan(sc, stream);
-    if (kr) return cuda_fail((cudaError_t)kr, "scan kernel");
-    kr = launch_scatter(dviews, T, sc, num_sms * 4, stream);
-    if (kr) return cuda_fail((cudaError_t)kr, "scatter kernel");
-    kr = launch_raster(dviews, T, sc, num_sms * tuning.ctas_per_sm, tuning.warps_per_cta, stream);
-    if (kr) return cuda_fail((cudaError_t)kr, "raster kernel");
-    launches += (vchunks.empty() ? 0 : 1) + (schunks.empty() ? 0 : 1) + (nscan > 0 ? 1 : 0) + 2;
-    Ctl* hctl = (Ctl*)(staging.base + host_bytes);
-    e = cudaMemcpyAsync(hctl, sc.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, stream);
-    if (e != cudaSuccess) return cuda_fail(e, "read control block");
-    e = cudaStreamSynchronize(stream);
+void Plan::bind(char* dev_base, char* host_base) {
+  dev = dev_base;
+  host = host_base;
+  for (int k = 0; k < n; k++) {
+    DView& v = views[k];
+    v.clip = (float4*)(dev + o_vout + offs[k].clip);
+    v.wpos = shader_needs_wpos(v.shader) ? (float4*)(dev + o_vout + offs[k].wpos) : nullptr;
+    v.wnrm = shader_needs_wnrm(v.shader) ? (float4*)(dev + o_vout + offs[k].wnrm) : nullptr;
+    v.clip_slot = (int32_t*)(dev + o_vout + offs[k].slot);
+  }
+  std::memcpy(host + o_views, views.data(), sizeof(DView) * n);
+  if (!vchunks.empty()) std::memcpy(host + o_vch, vchunks.data(), sizeof(Chunk) * vchunks.size());
+  if (!schunks.empty()) std::memcpy(host + o_sch, schunks.data(), sizeof(Chunk) * schunks.size());
+  sc.ctl = (Ctl*)(dev + o_ctl);
+  sc.view_done = (uint32_t*)(dev + o_done);
+  sc.recs = (RasterRec*)(dev + o_recs); sc.rec_cap = (uint32_t)rec_cap;
+  sc.pay = (Payload*)(dev + o_pay);
+  sc.clipbuf = (float*)(dev + o_clip); sc.clip_cap = (uint32_t)clip_cap;
+  sc.tile_count = (uint32_t*)(dev + o_cnt);
+  sc.tile_fill = (uint32_t*)(dev + o_fill);
+  sc.tile_off = (uint32_t*)(dev + o_toff);
+  sc.scan_status = (unsigned long long*)(dev + o_stat);
+  sc.bins = (uint32_t*)(dev + o_bins); sc.bin_cap = (uint32_t)bin_cap;
+  sc.ntiles = (int32_t)total_tiles;
+  sc.nviews = n;
+}
+
+// Upload of the view descriptors, one memset, five kernels, read-back of the control
+// block: everything stream-ordered, nothing synchronous (capturable into a CUDA graph).
+int Plan::enqueue(cudaStream_t s, int num_sms, const hsr_tuning& tu, cudaEvent_t* ev) {
+  const DView* dviews = (const DView*)(dev + o_views);
+  if (ev) cudaEventRecord(ev[0], s);
+  cudaError_t e = cudaMemcpyAsync(dev, host, host_bytes, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "upload views");
+  e = cudaMemsetAsync(dev + o_zero, 0, zero_bytes, s);
+  if (e != cudaSuccess) return cuda_fail(e, "clear scratch");
+  if (ev && ev[1]) cudaEventRecord(ev[1], s);
+  int kr = launch_vertex(dviews, (const Chunk*)(dev + o_vch), (int)vchunks.size(), s);
+  if (kr) return cuda_fail((cudaError_t)kr, "vertex kernel");
+  if (ev && ev[2]) cudaEventRecord(ev[2], s);
+  kr = launch_setup(dviews, (const Chunk*)(dev + o_sch), (int)schunks.size(), tile, sc, s);
+  if (kr) return cuda_fail((cudaError_t)kr, "setup kernel");
+  if (ev && ev[3]) cudaEventRecord(ev[3], s);
+  kr = launch_scan(sc, s);
+  if (kr) return cuda_fail((cudaError_t)kr, "scan kernel");
+  if (ev && ev[4]) cudaEventRecord(ev[4], s);
+  kr = launch_scatter(dviews, tile, sc, num_sms * 4, s);
+  if (kr) return cuda_fail((cudaError_t)kr, "scatter kernel");
+  if (ev && ev[5]) cudaEventRecord(ev[5], s);
+  kr = launch_raster(dviews, tile, sc, num_sms * tu.ctas_per_sm, tu.warps_per_cta, s);
+  if (kr) return cuda_fail((cudaError_t)kr, "raster kernel");
+  if (ev) cudaEventRecord(ev[6], s);
+  e = cudaMemcpyAsync(host + host_bytes, sc.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return cuda_fail(e, "read control block");
+  return HSR_OK;
+}
+
+int Plan::kernel_count() const {
+  return (vchunks.empty() ? 0 : 1) + (schunks.empty() ? 0 : 1) + (nscan > 0 ? 1 : 0) + 2;
+}
+
+// Grow the capacity an overflow reported; returns false if nothing overflowed.
+bool Plan::grow(const Ctl& c) {
+  if (!(c.error & (kErrRecOverflow | kErrClipOverflow | kErrBinOverflow))) return false;
+  if (c.error & kErrRecOverflow) rec_cap = std::max<size_t>(rec_cap * 2, (size_t)c.rec_count + 1024);
+  if (c.error & kErrClipOverflow) clip_cap = std::max<size_t>(clip_cap * 2, (size_t)c.clip_count + 256);
+  if (c.error & kErrBinOverflow) bin_cap = std::max<size_t>(bin_cap * 2, (size_t)c.bin_total + 4096);
+  return true;
+}
+
+void Runtime::record_result(const Plan& p, const Ctl& c) {
+  stats.records = c.rec_count;
+  stats.clipped_faces = c.clip_count;
+  stats.bin_pairs = c.bin_total;
+  stats.tiles = p.total_tiles;
+  timing.records = c.rec_count;
+  timing.bin_pairs = c.bin_total;
+  timing.shaded_pixels = c.shaded_px;
+  timing.pixels = p.total_pixels;
+  timing.faces = p.total_faces;
+  timing.vertices = p.total_pos;
+  timing.normals = p.total_nrm;
+  timing.clipped_faces = c.clip_count;
+  timing.launches = (uint32_t)p.kernel_count();
+  timing.h2d_bytes = p.host_bytes;
+  timing.d2h_bytes = sizeof(Ctl);
+  timing.views = (uint32_t)p.n;
+}
+
+int Runtime::run_batch(const hsr_draw_desc* descs, int n) {
+  if (n <= 0) return HSR_OK;
+  Plan p;
+  int rc = plan_build(descs, n, p);
+  if (rc != HSR_OK) return rc;
+  for (int attempt = 0; attempt < 6; attempt++) {
+    p.layout();
+    rc = arena.reserve(p.dev_bytes);
+    if (rc != HSR_OK) return rc;
+    rc = staging.reserve(p.stage_bytes);
+    if (rc != HSR_OK) return rc;
+    p.bind(arena.base, staging.base);
+    cudaEvent_t evs[7] = {ev[0], profiling ? ev[1] : nullptr, profiling ? ev[2] : nullptr,
+                          profiling ? ev[3] : nullptr, profiling ? ev[4] : nullptr,
+                          profiling ? ev[5] : nullptr, ev[6]};
+    rc = p.enqueue(stream, num_sms, tuning, evs);
+    if (rc != HSR_OK) return rc;
+    launches += (uint64_t)p.kernel_count();
+    cudaError_t e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) return cuda_fail(e, "draw batch");
-    const Ctl c = *hctl;
-    if (c.error & (kErrRecOverflow | kErrClipOverflow | kErrBinOverflow)) {
-      if (c.error & kErrRecOverflow) rec_cap = std::max<size_t>(rec_cap * 2, (size_t)c.rec_count + 1024);
-      if (c.error & kErrClipOverflow) clip_cap = std::max<size_t>(clip_cap * 2, (size_t)c.clip_count + 256);
-      if (c.error & kErrBinOverflow) bin_cap = std::max<size_t>(bin_cap * 2, (size_t)c.bin_total + 4096);
+    const Ctl c = *(const Ctl*)(p.host + p.host_bytes);
+    if (p.grow(c)) {
       stats.retries++;
-      cap_rec_hint = rec_cap; cap_clip_hint = clip_cap; cap_bin_hint = bin_cap;
+      cap_rec_hint = p.rec_cap; cap_clip_hint = p.clip_cap; cap_bin_hint = p.bin_cap;
       continue;
     }
     if (c.error & (kErrWaitTimeout | kErrScanTimeout))
       return fail(HSR_ERR_TIMEOUT, "draw batch: a bounded device wait gave up");
-    stats.records = c.rec_count;
-    stats.clipped_faces = c.clip_count;
-    stats.bin_pairs = c.bin_total;
-    stats.tiles = c.raster_tiles;
-    stats.kernel_launches = launches;
+    record_result(p, c);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev[0], ev[6]);
+    timing.batch_ms = ms;
+    for (int k = 0; k < 5; k++) {
+      float km = 0.f;
+      if (profiling) cudaEventElapsedTime(&km, ev[k + 1], ev[k + 2]);
+      timing.kernel_ms[k] = km;
+    }
     return HSR_OK;
   }
   return fail(HSR_ERR_BIN_OVERFLOW, "draw batch: scratch overflow persisted after retries");
@@ -403,6 +479,10 @@ int hsr_init(int device) {
   rt->num_sms = prop.multiProcessorCount;
   e = cudaStreamCreateWithFlags(&rt->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { delete rt; return cuda_fail(e, "cudaStreamCreate"); }
+  for (int k = 0; k < 7; k++) {
+    e = cudaEventCreate(&rt->ev[k]);
+    if (e != cudaSuccess) { delete rt; return cuda_fail(e, "cudaEventCreate"); }
+  }
   g_rt = rt;
   return HSR_OK;
 }
@@ -416,6 +496,7 @@ int hsr_shutdown(void) {
   for (auto& kv : g_rt->targets) delete kv.second;
   if (g_rt->arena.base) cudaFree(g_rt->arena.base);
   if (g_rt->staging.base) cudaFreeHost(g_rt->staging.base);
+  for (int k = 0; k < 7; k++) cudaEventDestroy(g_rt->ev[k]);
   cudaStreamDestroy(g_rt->stream);
   delete g_rt;
   g_rt = nullptr;
@@ -641,6 +722,36 @@ int hsr_set_tuning(const hsr_tuning* in) {
   if (!(in->bin_factor >= 0.5f && in->bin_factor <= 64.f)) return fail(HSR_ERR_INVALID_ARG, "set_tuning: bin_factor in [0.5,64]");
   g_rt->tuning = *in;
   return HSR_OK;
+}
+
+int hsr_set_profiling(int on) {
+  RT_OR_FAIL();
+  g_rt->profiling = on != 0;
+  return HSR_OK;
+}
+
+int hsr_last_timing(hsr_timing* out) {
+  RT_OR_FAIL();
+  if (!out) return fail(HSR_ERR_INVALID_ARG, "last_timing: null");
+  *out = g_rt->timing;
+  return HSR_OK;
+}
+
+int hsr_host_alloc(size_t bytes, void** out) {
+  if (!out) return fail(HSR_ERR_INVALID_ARG, "host_alloc: null");
+  *out = nullptr;
+  cudaError_t e = cudaMallocHost(out, bytes ? bytes : 1);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(HSR_ERR_OUT_OF_MEMORY, "host_alloc: cudaMallocHost failed");
+  }
+  return HSR_OK;
+}
+
+int hsr_host_free(void* p) {
+  if (!p) return HSR_OK;
+  cudaError_t e = cudaFreeHost(p);
+  return e == cudaSuccess ? HSR_OK : cuda_fail(e, "host_free");
 }
 
 int hsr_get_stats(hsr_stats* out) {

@@ -47,6 +47,30 @@ struct Pinned {  // grow-only pinned host staging
   int reserve(size_t bytes);
 };
 
+// One launch sequence: view descriptors, work chunks, scratch layout and capacities.
+struct Plan {
+  struct Off { size_t clip, wpos, wnrm, slot; };
+  int n = 0, tile = 8, nscan = 0;
+  std::vector<int> order;         // plan position -> index in the caller's array
+  std::vector<DView> views;
+  std::vector<Off> offs;
+  std::vector<Chunk> vchunks, schunks;
+  size_t view_bytes = 0, total_faces = 0, total_tiles = 0, total_pos = 0, total_nrm = 0, total_pixels = 0;
+  size_t rec_cap = 0, clip_cap = 0, bin_cap = 0;
+  size_t o_views = 0, o_vch = 0, o_sch = 0, o_vout = 0, o_zero = 0, zero_bytes = 0, o_ctl = 0, o_done = 0,
+         o_cnt = 0, o_fill = 0, o_stat = 0, o_toff = 0, o_recs = 0, o_pay = 0, o_clip = 0, o_bins = 0;
+  size_t dev_bytes = 0, host_bytes = 0, stage_bytes = 0;
+  char* dev = nullptr;
+  char* host = nullptr;
+  Scratch sc = {};
+
+  void layout();
+  void bind(char* dev_base, char* host_base);
+  int enqueue(cudaStream_t s, int num_sms, const hsr_tuning& tu, cudaEvent_t* ev);
+  int kernel_count() const;
+  bool grow(const Ctl& c);
+};
+
 struct Runtime {
   int device = 0;
   int num_sms = 1;
@@ -61,6 +85,9 @@ struct Runtime {
   hsr_stats stats = {};
   uint64_t launches = 0;
   size_t cap_rec_hint = 0, cap_clip_hint = 0, cap_bin_hint = 0;
+  bool profiling = false;
+  cudaEvent_t ev[7] = {};
+  hsr_timing timing = {};
 
   MeshObj* mesh(uint64_t h);
   TexObj* tex(uint64_t h);
@@ -68,6 +95,8 @@ struct Runtime {
   int validate(const hsr_draw_desc& d);
   int plan_order(const hsr_draw_desc* d, int n, std::vector<int>& order, std::vector<int>& dep0,
                  std::vector<int>& dep1);
+  int plan_build(const hsr_draw_desc* descs, int n, Plan& p);
+  void record_result(const Plan& p, const Ctl& c);
   int run_batch(const hsr_draw_desc* descs, int n);
   int clear_target(TargetObj* t, const uint8_t rgba[4], float depth);
 

@@ -5,7 +5,8 @@
 // k_scan    exclusive prefix sum of per-tile counts, single pass with decoupled look-back;
 //           block order comes from a ticket so a block only waits on blocks that already
 //           run, and every wait is bounded (error bit + give up, never a hang).
-// k_scatter writes record indices into the per-tile lists with warp-aggregated atomics.
+// k_scatter writes record indices into the per-tile lists with warp-aggregated atomics;
+//           a record touches at most kMaxRecordTiles tiles (setup splits larger ones).
 #include "hsr_device.cuh"
 
 namespace hsr {
@@ -134,8 +135,7 @@ __global__ void __launch_bounds__(256) k_scatter(const DView* __restrict__ views
       ntw = (int)(xr >> 16) / T - tx0 + 1;
       nt = ntw * ((int)(yr >> 16) / T - ty0 + 1);
     }
-    const bool big = nt > kBigRecordTiles;
-    const int my_n = big ? 0 : nt;
+    const int my_n = min(nt, kMaxRecordTiles);
     const int maxn = __reduce_max_sync(kFull, my_n);
     for (int k = 0; k < maxn; k++) {
       const int tile = (k < my_n) ? tbase + (ty0 + k / ntw) * tiles_x + tx0 + k % ntw : -1;
@@ -147,20 +147,6 @@ __global__ void __launch_bounds__(256) k_scatter(const DView* __restrict__ views
       if (tile >= 0) {
         const uint32_t pos = sc.tile_off[tile] + b + (uint32_t)__popc(grp & ((1u << lane) - 1u));
         if (pos < sc.bin_cap) sc.bins[pos] = i;
-      }
-    }
-    unsigned bm = __ballot_sync(kFull, big);
-    while (bm) {
-      const int l = __ffs(bm) - 1;
-      bm &= bm - 1;
-      const int btx0 = __shfl_sync(kFull, tx0, l), bty0 = __shfl_sync(kFull, ty0, l);
-      const int bntw = __shfl_sync(kFull, ntw, l), bnt = __shfl_sync(kFull, nt, l);
-      const int btb = __shfl_sync(kFull, tbase, l), btx = __shfl_sync(kFull, tiles_x, l);
-      const uint32_t rec = i0 + (uint32_t)l;
-      for (int k = lane; k < bnt; k += 32) {
-        const int tile = btb + (bty0 + k / bntw) * btx + btx0 + k % bntw;
-        const uint32_t pos = sc.tile_off[tile] + atomicAdd(&sc.tile_fill[tile], 1u);
-        if (pos < sc.bin_cap) sc.bins[pos] = rec;
       }
     }
   }

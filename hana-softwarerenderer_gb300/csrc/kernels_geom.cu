@@ -130,9 +130,59 @@ __device__ __forceinline__ void store_rec(RasterRec* dst, const RasterRec& r) {
   d[0] = s[0]; d[1] = s[1]; d[2] = s[2]; d[3] = s[3];
 }
 
-// Append the valid records of a warp and count the tiles each one touches.  All 32 lanes
-// of the warp must call this.
-__device__ void commit(bool valid, const RasterRec& r, const DView& v, int T, const Scratch& sc) {
+// Payload floats a shader reads, rounded up to whole float4s (see the Payload layout).
+__device__ __forceinline__ int payload_f4(int shader) {
+  switch (shader) {
+    case HSR_SHADER_FLAT: return 0;
+    case HSR_SHADER_SHADOW: case HSR_SHADER_GROUND: case HSR_SHADER_TOON: return 2;
+    case HSR_SHADER_TEXTURE: return 3;
+    case HSR_SHADER_TEXTURE_WITH_LIGHT: return 6;
+    default: return 8;
+  }
+}
+
+// Corner varyings c[k] in shader_struct_v2f order (13 floats) -> payload.
+__device__ __forceinline__ void make_payload(int shader, const float* c0, const float* c1, const float* c2,
+                                             Payload& p) {
+  const float* c[3] = {c0, c1, c2};
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    p.f[k] = fd(1.f, c[k][3]);                                   // recip_w (graphics.cpp:333-337)
+    p.f[3 + k] = shader == HSR_SHADER_SHADOW ? c[k][2] : c[k][12];
+    p.f[6 + 2 * k] = c[k][10];
+    p.f[7 + 2 * k] = c[k][11];
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      p.f[12 + 3 * k + q] = c[k][7 + q];
+      p.f[21 + 3 * k + q] = c[k][4 + q];
+    }
+  }
+  p.f[30] = 0.f;
+  p.f[31] = 0.f;
+}
+
+__device__ __forceinline__ void store_payload(Payload* dst, const Payload& p, int nf4) {
+  float4* d = reinterpret_cast<float4*>(dst);
+  const float4* s = reinterpret_cast<const float4*>(&p);
+#pragma unroll
+  for (int q = 0; q < 8; q++)
+    if (q < nf4) d[q] = s[q];
+}
+
+__device__ __forceinline__ void rec_tiles(const RasterRec& r, int T, int& tx0, int& ty0, int& ntw, int& nt) {
+  const int x0 = (int)(r.xr & 0xffffu), x1 = (int)(r.xr >> 16);
+  const int y0 = (int)(r.yr & 0xffffu), y1 = (int)(r.yr >> 16);
+  tx0 = x0 / T;
+  ty0 = y0 / T;
+  ntw = x1 / T - tx0 + 1;
+  nt = ntw * (y1 / T - ty0 + 1);
+}
+
+// Append the records of a warp (at most one per lane, each touching <= kMaxRecordTiles
+// tiles) and count the tiles they touch, aggregating equal tiles across lanes.  All 32
+// lanes call this.
+__device__ void append_small(bool valid, const RasterRec& r, const Payload& pl, int nf4, const DView& v, int T,
+                             const Scratch& sc) {
   const int lane = threadIdx.x & 31;
   const unsigned m = __ballot_sync(kFull, valid);
   if (!m) return;
@@ -141,34 +191,76 @@ __device__ void commit(bool valid, const RasterRec& r, const DView& v, int T, co
   if (lane == leader) base = atomicAdd(&sc.ctl->rec_count, (uint32_t)__popc(m));
   base = __shfl_sync(kFull, base, leader);
   const uint32_t slot = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
-  bool ok = valid && slot < sc.rec_cap;
+  const bool ok = valid && slot < sc.rec_cap;
   if (valid && !ok) atomicOr(&sc.ctl->error, kErrRecOverflow);
-  if (ok) store_rec(&sc.recs[slot], r);
-
-  int tx0 = 0, ty0 = 0, ntw = 0, nt = 0;
+  int tx0 = 0, ty0 = 0, ntw = 1, nt = 0;
   if (ok) {
-    const int x0 = (int)(r.xr & 0xffffu), x1 = (int)(r.xr >> 16);
-    const int y0 = (int)(r.yr & 0xffffu), y1 = (int)(r.yr >> 16);
-    tx0 = x0 / T; ty0 = y0 / T;
-    ntw = x1 / T - tx0 + 1;
-    nt = ntw * (y1 / T - ty0 + 1);
+    RasterRec w = r;
+    w.pad = slot;  // payload index
+    store_rec(&sc.recs[slot], w);
+    store_payload(&sc.pay[slot], pl, nf4);
+    rec_tiles(r, T, tx0, ty0, ntw, nt);
   }
-  const bool big = nt > kBigRecordTiles;
-  const int my_n = big ? 0 : nt;
-  const int maxn = __reduce_max_sync(kFull, my_n);
+  const int maxn = __reduce_max_sync(kFull, nt);
   for (int k = 0; k < maxn; k++) {
-    const int tile = (k < my_n) ? v.tile_base + (ty0 + k / ntw) * v.tiles_x + tx0 + k % ntw : -1;
+    const int tile = (k < nt) ? v.tile_base + (ty0 + k / ntw) * v.tiles_x + tx0 + k % ntw : -1;
     const unsigned grp = __match_any_sync(kFull, tile);
     if (tile >= 0 && lane == __ffs(grp) - 1) atomicAdd(&sc.tile_count[tile], (uint32_t)__popc(grp));
   }
+}
+
+// Emit the records of a warp.  A triangle whose bounding box touches more than
+// kMaxRecordTiles tiles becomes sub-records over blocks of kSubTilesX x kSubTilesY tiles:
+// same triangle constants and seq, pixel range clipped to the block, payload shared with
+// the first sub-record.  The union of the sub-ranges is the triangle's pixel range, so
+// every covered pixel is still tested exactly once.
+__device__ void commit(bool valid, const RasterRec& r, const Payload& pl, const DView& v, int T,
+                       const Scratch& sc) {
+  const int lane = threadIdx.x & 31;
+  const int nf4 = payload_f4(v.shader);
+  int tx0 = 0, ty0 = 0, ntw = 1, nt = 0;
+  if (valid) rec_tiles(r, T, tx0, ty0, ntw, nt);
+  const bool big = valid && nt > kMaxRecordTiles;
+  append_small(valid && !big, r, pl, nf4, v, T, sc);
+
   unsigned bm = __ballot_sync(kFull, big);
   while (bm) {
     const int l = __ffs(bm) - 1;
     bm &= bm - 1;
+    RasterRec b;
+    {
+      const uint32_t* src = reinterpret_cast<const uint32_t*>(&r);
+      uint32_t* dst = reinterpret_cast<uint32_t*>(&b);
+#pragma unroll
+      for (int q = 0; q < 16; q++) dst[q] = __shfl_sync(kFull, src[q], l);
+    }
     const int btx0 = __shfl_sync(kFull, tx0, l), bty0 = __shfl_sync(kFull, ty0, l);
     const int bntw = __shfl_sync(kFull, ntw, l), bnt = __shfl_sync(kFull, nt, l);
-    for (int k = lane; k < bnt; k += 32)
-      atomicAdd(&sc.tile_count[v.tile_base + (bty0 + k / bntw) * v.tiles_x + btx0 + k % bntw], 1u);
+    const int bnth = bnt / bntw;
+    const int nbx = (bntw + kSubTilesX - 1) / kSubTilesX, nby = (bnth + kSubTilesY - 1) / kSubTilesY;
+    const int nsub = nbx * nby;
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(&sc.ctl->rec_count, (uint32_t)nsub);
+    base = __shfl_sync(kFull, base, 0);
+    if ((uint64_t)base + (uint64_t)nsub > (uint64_t)sc.rec_cap) {
+      if (lane == 0) atomicOr(&sc.ctl->error, kErrRecOverflow);
+      continue;
+    }
+    if (lane == l) store_payload(&sc.pay[base], pl, nf4);
+    const int x0 = (int)(b.xr & 0xffffu), x1 = (int)(b.xr >> 16);
+    const int y0 = (int)(b.yr & 0xffffu), y1 = (int)(b.yr >> 16);
+    for (int sidx = lane; sidx < nsub; sidx += 32) {
+      const int bx = sidx % nbx, by = sidx / nbx;
+      const int stx0 = btx0 + bx * kSubTilesX, stx1 = min(btx0 + bntw - 1, stx0 + kSubTilesX - 1);
+      const int sty0 = bty0 + by * kSubTilesY, sty1 = min(bty0 + bnth - 1, sty0 + kSubTilesY - 1);
+      RasterRec w = b;
+      w.xr = (uint32_t)max(x0, stx0 * T) | ((uint32_t)min(x1, stx1 * T + T - 1) << 16);
+      w.yr = (uint32_t)max(y0, sty0 * T) | ((uint32_t)min(y1, sty1 * T + T - 1) << 16);
+      w.pad = base;
+      store_rec(&sc.recs[base + (uint32_t)sidx], w);
+      for (int ty = sty0; ty <= sty1; ty++)
+        for (int tx = stx0; tx <= stx1; tx++) atomicAdd(&sc.tile_count[v.tile_base + ty * v.tiles_x + tx], 1u);
+    }
   }
 }
 
@@ -218,15 +310,38 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const DView* __restrict
   // ---- fast accept (graphics.cpp:140-148) ---------------------------------------------
   bool needs_clip = false, valid = false;
   RasterRec r;
+  Payload pl;
   if (active) {
     const int4 iv = __ldg(&v.fv[f]);
     const float4 c0 = v.clip[iv.x], c1 = v.clip[iv.y], c2 = v.clip[iv.z];
-    if (vertex_visible(c0) && vertex_visible(c1) && vertex_visible(c2))
+    if (vertex_visible(c0) && vertex_visible(c1) && vertex_visible(c2)) {
       valid = build_rec(v, c0, c1, c2, (uint32_t)f << 4, (uint32_t)ch.view, r);
-    else
+      if (valid && payload_f4(v.shader) > 0) {
+        // corner varyings of the three vertex() calls, in shader_struct_v2f order
+        float c[3][kVaryings];
+        const int pi[3] = {iv.x, iv.y, iv.z};
+        const float4 cl[3] = {c0, c1, c2};
+        int4 it = make_int4(0, 0, 0, 0), in = make_int4(0, 0, 0, 0);
+        if (v.uv) it = __ldg(&v.fvt[f]);
+        if (v.wnrm) in = __ldg(&v.fvn[f]);
+        const int ti[3] = {it.x, it.y, it.z}, ni[3] = {in.x, in.y, in.z};
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          c[k][0] = cl[k].x; c[k][1] = cl[k].y; c[k][2] = cl[k].z; c[k][3] = cl[k].w;
+          const float4 wp = v.wpos ? v.wpos[pi[k]] : make_float4(0.f, 0.f, 0.f, 0.f);
+          const float4 wn = v.wnrm ? v.wnrm[ni[k]] : make_float4(0.f, 0.f, 0.f, 0.f);
+          const float2 t = (v.uv && payload_f4(v.shader) >= 3) ? __ldg(&v.uv[ti[k]]) : make_float2(0.f, 0.f);
+          c[k][4] = wp.x; c[k][5] = wp.y; c[k][6] = wp.z;
+          c[k][7] = wn.x; c[k][8] = wn.y; c[k][9] = wn.z;
+          c[k][10] = t.x; c[k][11] = t.y; c[k][12] = wn.w;
+        }
+        make_payload(v.shader, c[0], c[1], c[2], pl);
+      }
+    } else {
       needs_clip = true;
+    }
   }
-  commit(valid, r, v, T, sc);
+  commit(valid, r, pl, v, T, sc);
 
   // ---- homogeneous clipping, one face at a time per warp (graphics.cpp:73-161) ---------
   unsigned cm = __ballot_sync(kFull, needs_clip);
@@ -277,6 +392,7 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const DView* __restrict
     }
     bool cvalid = false;
     RasterRec cr;
+    Payload cpl;
     if (n >= 3) {
       uint32_t slot = 0;
       if (lane == 0) slot = atomicAdd(&sc.ctl->clip_count, 1u);
@@ -295,12 +411,13 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const DView* __restrict
           cvalid = build_rec(v, make_float4(p0[0], p0[1], p0[2], p0[3]), make_float4(p1[0], p1[1], p1[2], p1[3]),
                              make_float4(p2[0], p2[1], p2[2], p2[3]),
                              ((uint32_t)face << 4) | ((uint32_t)lane << 1) | 1u, (uint32_t)ch.view, cr);
+          if (cvalid) make_payload(v.shader, p0, p1, p2, cpl);
         }
       } else if (lane == 0) {
         atomicOr(&sc.ctl->error, kErrClipOverflow);
       }
     }
-    commit(cvalid, cr, v, T, sc);
+    commit(cvalid, cr, cpl, v, T, sc);
     __syncwarp();
   }
 }

@@ -35,71 +35,6 @@ __device__ __forceinline__ float canon_depth(float d) {
   return d != d ? __int_as_float(0x7f800000) : d;
 }
 
-struct Corner {
-  float w, clip_z;
-  F3 wpos, wnrm;
-  float u, t, intensity;
-};
-
-__device__ __forceinline__ void load_corners(const DView& v, const Scratch& sc, uint32_t seq, Corner c[3]) {
-  const int face = (int)(seq >> 4);
-  if (!(seq & 1u)) {
-    const int4 iv = __ldg(&v.fv[face]);
-    const int pi[3] = {iv.x, iv.y, iv.z};
-    int ti[3] = {0, 0, 0}, ni[3] = {0, 0, 0};
-    if (needs_uv(v.shader)) {
-      const int4 it = __ldg(&v.fvt[face]);
-      ti[0] = it.x; ti[1] = it.y; ti[2] = it.z;
-    }
-    if (needs_wnrm(v.shader)) {
-      const int4 in = __ldg(&v.fvn[face]);
-      ni[0] = in.x; ni[1] = in.y; ni[2] = in.z;
-    }
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      const float4 cl = v.clip[pi[k]];
-      c[k].w = cl.w;
-      c[k].clip_z = cl.z;
-      if (needs_wpos(v.shader)) {
-        const float4 p = v.wpos[pi[k]];
-        c[k].wpos = {p.x, p.y, p.z};
-      } else {
-        c[k].wpos = {0.f, 0.f, 0.f};
-      }
-      if (needs_wnrm(v.shader)) {
-        const float4 n = v.wnrm[ni[k]];
-        c[k].wnrm = {n.x, n.y, n.z};
-        c[k].intensity = n.w;
-      } else {
-        c[k].wnrm = {0.f, 0.f, 0.f};
-        c[k].intensity = 0.f;
-      }
-      if (needs_uv(v.shader)) {
-        const float2 t = __ldg(&v.uv[ti[k]]);
-        c[k].u = t.x; c[k].t = t.y;
-      } else {
-        c[k].u = c[k].t = 0.f;
-      }
-    }
-  } else {
-    // clipped face: fan triangle (0, j+1, j+2) of the stored polygon (graphics.cpp:394-405)
-    const int fan = (int)((seq >> 1) & 7u);
-    const int slot = v.clip_slot[face];
-    const float* P = sc.clipbuf + (size_t)slot * kClipSlotFloats + 4;
-    const int vi[3] = {0, fan + 1, fan + 2};
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      const float* q = P + vi[k] * kVaryings;
-      c[k].w = q[3];
-      c[k].clip_z = q[2];
-      c[k].wpos = {q[4], q[5], q[6]};
-      c[k].wnrm = {q[7], q[8], q[9]};
-      c[k].u = q[10]; c[k].t = q[11];
-      c[k].intensity = q[12];
-    }
-  }
-}
-
 // interpolate_varyings (graphics.cpp:205-220) for one float
 __device__ __forceinline__ float interp(float s0, float s1, float s2, float w0, float w1, float w2, float nrm) {
   return fm(fa(fa(fm(s0, w0), fm(s1, w1)), fm(s2, w2)), nrm);
@@ -115,29 +50,37 @@ __device__ __forceinline__ void bary(const RasterRec& r, float px, float py, flo
   b2 = fd(ux, r.uz);
 }
 
-__device__ __forceinline__ uint32_t shade_pixel(const DView& v, const Scratch& sc, const RasterRec& r, int x, int y,
+// Shade one pixel from its winning record and that record's payload (Payload layout in
+// hsr_internal.h): perspective-correct varyings, then the fragment shader.
+__device__ __forceinline__ uint32_t shade_pixel(const DView& v, const RasterRec& r, const float* P, int x, int y,
                                                 uint32_t alpha_word) {
+  const uint32_t prim = v.prim_base + (r.seq >> 4) + 1u;
+  if (v.shader == HSR_SHADER_FLAT) return pack_rgb(fragment(v, Frag{}, prim), alpha_word);
   float b0, b1, b2;
   bary(r, (float)x, (float)y, b0, b1, b2);
-  Corner c[3];
-  load_corners(v, sc, r.seq, c);
-  const float w0 = fm(fd(1.f, c[0].w), b0);
-  const float w1 = fm(fd(1.f, c[1].w), b1);
-  const float w2 = fm(fd(1.f, c[2].w), b2);
+  const float w0 = fm(P[0], b0), w1 = fm(P[1], b1), w2 = fm(P[2], b2);
   const float nrm = fd(1.f, fa(fa(w0, w1), w2));
   Frag f;
-  f.clip_z = interp(c[0].clip_z, c[1].clip_z, c[2].clip_z, w0, w1, w2, nrm);
-  f.wpos = {interp(c[0].wpos.x, c[1].wpos.x, c[2].wpos.x, w0, w1, w2, nrm),
-            interp(c[0].wpos.y, c[1].wpos.y, c[2].wpos.y, w0, w1, w2, nrm),
-            interp(c[0].wpos.z, c[1].wpos.z, c[2].wpos.z, w0, w1, w2, nrm)};
-  f.wnrm = {interp(c[0].wnrm.x, c[1].wnrm.x, c[2].wnrm.x, w0, w1, w2, nrm),
-            interp(c[0].wnrm.y, c[1].wnrm.y, c[2].wnrm.y, w0, w1, w2, nrm),
-            interp(c[0].wnrm.z, c[1].wnrm.z, c[2].wnrm.z, w0, w1, w2, nrm)};
-  f.u = interp(c[0].u, c[1].u, c[2].u, w0, w1, w2, nrm);
-  f.t = interp(c[0].t, c[1].t, c[2].t, w0, w1, w2, nrm);
-  f.intensity = interp(c[0].intensity, c[1].intensity, c[2].intensity, w0, w1, w2, nrm);
-  const uint32_t prim = v.prim_base + (r.seq >> 4) + 1u;
+  const float sc = interp(P[3], P[4], P[5], w0, w1, w2, nrm);
+  f.clip_z = sc;
+  f.intensity = sc;
+  f.u = interp(P[6], P[8], P[10], w0, w1, w2, nrm);
+  f.t = interp(P[7], P[9], P[11], w0, w1, w2, nrm);
+  f.wnrm = {interp(P[12], P[15], P[18], w0, w1, w2, nrm), interp(P[13], P[16], P[19], w0, w1, w2, nrm),
+            interp(P[14], P[17], P[20], w0, w1, w2, nrm)};
+  f.wpos = {interp(P[21], P[24], P[27], w0, w1, w2, nrm), interp(P[22], P[25], P[28], w0, w1, w2, nrm),
+            interp(P[23], P[26], P[29], w0, w1, w2, nrm)};
   return pack_rgb(fragment(v, f, prim), alpha_word);
+}
+
+__device__ __forceinline__ int payload_f4_r(int shader) {
+  switch (shader) {
+    case HSR_SHADER_FLAT: return 0;
+    case HSR_SHADER_SHADOW: case HSR_SHADER_GROUND: case HSR_SHADER_TOON: return 2;
+    case HSR_SHADER_TEXTURE: return 3;
+    case HSR_SHADER_TEXTURE_WITH_LIGHT: return 6;
+    default: return 8;
+  }
 }
 
 __device__ __forceinline__ int find_view(const DView* views, int nviews, int t) {
@@ -164,11 +107,13 @@ __device__ __forceinline__ void wait_view(const Scratch& sc, const DView* views,
 }
 
 template <int T, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) k_raster(const DView* __restrict__ views, Scratch sc) {
+__global__ void __launch_bounds__(WARPS * 32, T == 32 ? 2 : 32 / WARPS) k_raster(const DView* __restrict__ views, Scratch sc) {
   constexpr int RP = 32 / T;        // rows covered by one pass of the warp
   constexpr int PPL = T * T / 32;   // pixels per lane
   __shared__ RasterRec srec[WARPS][32];
+  __shared__ uint32_t sidx[WARPS][32];
   __shared__ uint32_t swin[WARPS][T * T];
+  __shared__ uint32_t spay[WARPS][T * T];
   __shared__ float sz[WARPS][T * T];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (sc.ctl->error & (kErrBinOverflow | kErrRecOverflow | kErrClipOverflow | kErrScanTimeout)) return;
@@ -209,7 +154,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(const DView* __restrict__
       }
     } else {
       float cz[PPL];
-      uint32_t cs[PPL], cw[PPL];
+      uint32_t cs[PPL], cw[PPL], cp[PPL];
 #pragma unroll
       for (int k = 0; k < PPL; k++) {
         const int y = ybase + k * RP;
@@ -218,6 +163,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(const DView* __restrict__
         cz[k] = canon_depth(d);
         cs[k] = 0u;
         cw[k] = 0u;
+        cp[k] = 0u;
       }
       const uint32_t off = sc.tile_off[t];
       const float pxf = (float)x;
@@ -228,7 +174,6 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(const DView* __restrict__
           RasterRec rr;
           if (ri < nrec) {
             rr = sc.recs[ri];
-            rr.pad = ri;  // keep the record index beside the record
           } else {        // never produced by a consistent bin pass; covers no pixel
             rr.xr = 1u;
             rr.yr = 1u;
@@ -237,6 +182,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(const DView* __restrict__
             rr.pad = 0u;
           }
           srec[warp][lane] = rr;
+          sidx[warp][lane] = ri;
         }
         __syncwarp();
         for (uint32_t j = 0; j < cnt; j++) {
@@ -277,7 +223,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(const DView* __restrict__
             if (z < cz[k] || (z == cz[k] && seqp1 > cs[k])) {
               cz[k] = z;
               cs[k] = seqp1;
-              cw[k] = r.pad;
+              cw[k] = sidx[warp][j];
+              cp[k] = r.pad;
             }
           }
         }
@@ -287,9 +234,12 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(const DView* __restrict__
 #pragma unroll
       for (int k = 0; k < PPL; k++) {
         swin[warp][k * 32 + lane] = cs[k] ? cw[k] : 0xffffffffu;
+        spay[warp][k * 32 + lane] = cp[k];
         sz[warp][k * 32 + lane] = cz[k];
       }
       __syncwarp();
+      uint32_t shaded = 0;
+      const int nf4 = payload_f4_r(v.shader);
 #pragma unroll 1
       for (int k = 0; k < PPL; k++) {
         const int y = ybase + k * RP;
@@ -297,9 +247,18 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(const DView* __restrict__
         const size_t idx = (size_t)y * v.W + x;
         const uint32_t w = swin[warp][k * 32 + lane];
         if (w != 0xffffffffu) {
+          shaded++;
           const RasterRec r = sc.recs[w];
+          float P[kPayloadFloats];
+          {
+            const float4* src = reinterpret_cast<const float4*>(&sc.pay[spay[warp][k * 32 + lane]]);
+            float4* dst = reinterpret_cast<float4*>(P);
+#pragma unroll
+            for (int q = 0; q < kPayloadFloats / 4; q++)
+              dst[q] = q < nf4 ? src[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+          }
           const uint32_t alpha = clear ? v.clear_rgba : __ldcg(&v.color[idx]);
-          v.color[idx] = shade_pixel(v, sc, r, x, y, alpha);
+          v.color[idx] = shade_pixel(v, r, P, x, y, alpha);
           v.depth[idx] = sz[warp][k * 32 + lane];
           if (v.prim) v.prim[idx] = v.prim_base + (r.seq >> 4) + 1u;
         } else if (clear) {
@@ -308,13 +267,15 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(const DView* __restrict__
           if (v.prim) v.prim[idx] = 0u;
         }
       }
+      shaded = __reduce_add_sync(kFull, shaded);
+      if (lane == 0 && shaded) atomicAdd(&sc.ctl->shaded_px, (unsigned long long)shaded);
       __syncwarp();
     }
-    __threadfence();
-    __syncwarp();
-    if (lane == 0) {
-      atomicAdd(&sc.view_done[vi], 1u);
-      atomicAdd(&sc.ctl->raster_tiles, 1u);
+    if (v.has_dependents) {
+      // publish this tile's writes before counting it done (a later view reads them)
+      __threadfence();
+      __syncwarp();
+      if (lane == 0) atomicAdd(&sc.view_done[vi], 1u);
     }
   }
 }

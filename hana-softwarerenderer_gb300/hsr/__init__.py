@@ -46,6 +46,17 @@ class Tuning(ctypes.Structure):
                 ("bin_factor", ctypes.c_float)]
 
 
+class Timing(ctypes.Structure):
+    _fields_ = [("batch_ms", ctypes.c_float), ("kernel_ms", ctypes.c_float * 5), ("launches", ctypes.c_uint32),
+                ("views", ctypes.c_uint32), ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
+                ("pixels", ctypes.c_uint64), ("shaded_pixels", ctypes.c_uint64), ("records", ctypes.c_uint64),
+                ("bin_pairs", ctypes.c_uint64), ("faces", ctypes.c_uint64), ("vertices", ctypes.c_uint64),
+                ("normals", ctypes.c_uint64), ("clipped_faces", ctypes.c_uint64)]
+
+
+KERNELS = ("vertex", "setup", "scan", "scatter", "raster")
+
+
 class Stats(ctypes.Structure):
     _fields_ = [("records", ctypes.c_uint64), ("clipped_faces", ctypes.c_uint64), ("bin_pairs", ctypes.c_uint64),
                 ("tiles", ctypes.c_uint64), ("retries", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64)]
@@ -88,6 +99,10 @@ def lib():
         "hsr_get_tuning": ([ctypes.POINTER(Tuning)], ctypes.c_int),
         "hsr_set_tuning": ([ctypes.POINTER(Tuning)], ctypes.c_int),
         "hsr_get_stats": ([ctypes.POINTER(Stats)], ctypes.c_int),
+        "hsr_set_profiling": ([ctypes.c_int], ctypes.c_int),
+        "hsr_last_timing": ([ctypes.POINTER(Timing)], ctypes.c_int),
+        "hsr_host_alloc": ([ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+        "hsr_host_free": ([ctypes.c_void_p], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -137,6 +152,37 @@ def stats() -> dict:
     s = Stats()
     check(lib().hsr_get_stats(ctypes.byref(s)))
     return {k: int(getattr(s, k)) for k, _ in Stats._fields_}
+
+
+def set_profiling(on: bool) -> None:
+    check(lib().hsr_set_profiling(1 if on else 0))
+
+
+def last_timing() -> dict:
+    t = Timing()
+    check(lib().hsr_last_timing(ctypes.byref(t)))
+    d = {k: (list(getattr(t, k)) if k == "kernel_ms" else getattr(t, k)) for k, _ in Timing._fields_}
+    d["kernel_ms"] = dict(zip(KERNELS, d["kernel_ms"]))
+    return d
+
+
+class PinnedArray:
+    """numpy view of page-locked host memory from hsr_host_alloc (freed on release())."""
+
+    def __init__(self, shape, dtype):
+        dtype = np.dtype(dtype)
+        n = int(np.prod(shape)) * dtype.itemsize
+        p = ctypes.c_void_p()
+        check(lib().hsr_host_alloc(n, ctypes.byref(p)))
+        self.ptr = p.value
+        buf = (ctypes.c_uint8 * n).from_address(self.ptr)
+        self.array = np.frombuffer(buf, dtype=dtype).reshape(shape)
+
+    def release(self) -> None:
+        if self.ptr:
+            self.array = None
+            check(lib().hsr_host_free(ctypes.c_void_p(self.ptr)))
+            self.ptr = None
 
 
 class Mesh:

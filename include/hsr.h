@@ -178,6 +178,32 @@ typedef struct hsr_stats {
 } hsr_stats;
 HSR_API int hsr_get_stats(hsr_stats* out);
 
+/* ---- timing of the last completed draw sequence (CUDA events on the library stream) --
+ * batch_ms spans the upload of the view descriptors to the end of the raster kernel;
+ * kernel_ms = {vertex, setup, scan, scatter, raster}, filled when profiling is on. */
+typedef struct hsr_timing {
+  float batch_ms;
+  float kernel_ms[5];
+  uint32_t launches;       /* kernels launched by the sequence                         */
+  uint32_t views;          /* draws in the sequence                                    */
+  uint64_t h2d_bytes;      /* host -> device bytes of the sequence (view descriptors)  */
+  uint64_t d2h_bytes;      /* device -> host bytes (control block)                     */
+  uint64_t pixels;         /* target pixels covered by the draws' tile grids           */
+  uint64_t shaded_pixels;  /* pixels whose visible fragment was shaded                 */
+  uint64_t records;        /* triangles that reached the raster                        */
+  uint64_t bin_pairs;      /* (triangle, tile) pairs                                   */
+  uint64_t faces;          /* faces processed                                          */
+  uint64_t vertices;       /* positions transformed                                    */
+  uint64_t normals;        /* normals transformed                                      */
+  uint64_t clipped_faces;  /* faces that went through the homogeneous clipper          */
+} hsr_timing;
+HSR_API int hsr_set_profiling(int on);
+HSR_API int hsr_last_timing(hsr_timing* out);
+
+/* Page-locked host memory for buffers passed to upload / download (fast DMA). */
+HSR_API int hsr_host_alloc(size_t bytes, void** out);
+HSR_API int hsr_host_free(void* p);
+
 #ifdef __cplusplus
 }
 #endif
