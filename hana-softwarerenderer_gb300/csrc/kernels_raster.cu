@@ -113,7 +113,6 @@ __global__ void __launch_bounds__(WARPS * 32, T == 32 ? 2 : 32 / WARPS) k_raster
   __shared__ RasterRec srec[WARPS][32];
   __shared__ uint32_t sidx[WARPS][32];
   __shared__ uint32_t swin[WARPS][T * T];
-  __shared__ uint32_t spay[WARPS][T * T];
   __shared__ float sz[WARPS][T * T];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (sc.ctl->error & (kErrBinOverflow | kErrRecOverflow | kErrClipOverflow | kErrScanTimeout)) return;
@@ -154,7 +153,7 @@ __global__ void __launch_bounds__(WARPS * 32, T == 32 ? 2 : 32 / WARPS) k_raster
       }
     } else {
       float cz[PPL];
-      uint32_t cs[PPL], cw[PPL], cp[PPL];
+      uint32_t cs[PPL], cw[PPL];
 #pragma unroll
       for (int k = 0; k < PPL; k++) {
         const int y = ybase + k * RP;
@@ -163,7 +162,6 @@ __global__ void __launch_bounds__(WARPS * 32, T == 32 ? 2 : 32 / WARPS) k_raster
         cz[k] = canon_depth(d);
         cs[k] = 0u;
         cw[k] = 0u;
-        cp[k] = 0u;
       }
       const uint32_t off = sc.tile_off[t];
       const float pxf = (float)x;
@@ -224,7 +222,6 @@ __global__ void __launch_bounds__(WARPS * 32, T == 32 ? 2 : 32 / WARPS) k_raster
               cz[k] = z;
               cs[k] = seqp1;
               cw[k] = sidx[warp][j];
-              cp[k] = r.pad;
             }
           }
         }
@@ -234,7 +231,6 @@ __global__ void __launch_bounds__(WARPS * 32, T == 32 ? 2 : 32 / WARPS) k_raster
 #pragma unroll
       for (int k = 0; k < PPL; k++) {
         swin[warp][k * 32 + lane] = cs[k] ? cw[k] : 0xffffffffu;
-        spay[warp][k * 32 + lane] = cp[k];
         sz[warp][k * 32 + lane] = cz[k];
       }
       __syncwarp();
@@ -248,14 +244,22 @@ __global__ void __launch_bounds__(WARPS * 32, T == 32 ? 2 : 32 / WARPS) k_raster
         const uint32_t w = swin[warp][k * 32 + lane];
         if (w != 0xffffffffu) {
           shaded++;
+          // the payload index equals the record index except for sub-records of a split
+          // triangle: load both at once, reload the payload in that rare case
           const RasterRec r = sc.recs[w];
           float P[kPayloadFloats];
           {
-            const float4* src = reinterpret_cast<const float4*>(&sc.pay[spay[warp][k * 32 + lane]]);
             float4* dst = reinterpret_cast<float4*>(P);
+            const float4* src = reinterpret_cast<const float4*>(&sc.pay[w]);
 #pragma unroll
             for (int q = 0; q < kPayloadFloats / 4; q++)
               dst[q] = q < nf4 ? src[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+            if (r.pad != w) {
+              src = reinterpret_cast<const float4*>(&sc.pay[r.pad]);
+#pragma unroll
+              for (int q = 0; q < kPayloadFloats / 4; q++)
+                dst[q] = q < nf4 ? src[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
           }
           const uint32_t alpha = clear ? v.clear_rgba : __ldcg(&v.color[idx]);
           v.color[idx] = shade_pixel(v, r, P, x, y, alpha);
