@@ -21,7 +21,6 @@ namespace hsr {
 
 constexpr int kMaxPoly = 10;              // 3 vertices + one per clip plane (7 planes)
 constexpr int kVaryings = 13;             // floats in shader_struct_v2f (IShader.h:41-47)
-constexpr int kClipSlotFloats = 4 + kMaxPoly * kVaryings + 2;  // n, pad[3], verts, pad -> 136
 constexpr int kMaxRecordTiles = 32;       // records never touch more tiles (big ones are split)
 constexpr int kSubTilesX = 8, kSubTilesY = 4;  // tile block of one sub-record
 constexpr int kPayloadFloats = 32;        // per-record shading payload (see Payload layout)
@@ -33,7 +32,9 @@ enum : uint32_t {
   kErrBinOverflow = 4u,
   kErrWaitTimeout = 8u,
   kErrScanTimeout = 16u,
+  kErrBigOverflow = 32u,
 };
+constexpr uint32_t kErrCapacity = kErrRecOverflow | kErrClipOverflow | kErrBinOverflow | kErrBigOverflow;
 
 // Record flags.
 enum : uint32_t {
@@ -76,7 +77,6 @@ struct DView {
   float4* clip;   // [npos]
   float4* wpos;   // [npos] or null
   float4* wnrm;   // [nnrm] (xyz, intensity) or null
-  int32_t* clip_slot;  // [nfaces]: slot in the clip buffer, written for clipped faces only
   // shading
   int32_t shader;
   uint32_t flags;       // HSR_DRAW_*
@@ -105,9 +105,16 @@ struct Ctl {
   uint32_t scan_ticket;
   uint32_t error;
   uint32_t bin_total;
-  uint32_t raster_tiles;
-  uint32_t pad;
+  uint32_t big_count;      // triangles queued for sub-record expansion
+  uint32_t post_next;      // work counter of k_post
   unsigned long long shaded_px;  // pixels whose winner was shaded by the raster
+};
+
+// A triangle whose bounding box touches more than kMaxRecordTiles tiles, queued by setup
+// and expanded into sub-records by k_post.
+struct __align__(16) BigItem {
+  RasterRec rec;
+  Payload pay;
 };
 
 // Work chunk for the vertex and setup kernels: items [begin, end) of one view.
@@ -124,7 +131,8 @@ struct Scratch {
   uint32_t* view_done;      // [nviews] tiles finished per view
   RasterRec* recs;  uint32_t rec_cap;
   Payload* pay;             // [rec_cap]
-  float* clipbuf;   uint32_t clip_cap;   // kClipSlotFloats per slot
+  int2* clipq;      uint32_t clip_cap;   // (view, face) of faces that need clipping
+  BigItem* bigq;    uint32_t big_cap;
   uint32_t* tile_count;     // [ntiles]
   uint32_t* tile_fill;      // [ntiles]
   uint32_t* tile_off;       // [ntiles]
@@ -137,6 +145,7 @@ struct Scratch {
 // Kernel launchers (kernels_*.cu).  All return cudaError_t as int.
 int launch_vertex(const DView* views, const Chunk* chunks, int nchunks, cudaStream_t s);
 int launch_setup(const DView* views, const Chunk* chunks, int nchunks, int tile, Scratch sc, cudaStream_t s);
+int launch_post(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s);
 int launch_scan(Scratch sc, cudaStream_t s);
 int launch_scatter(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s);
 int launch_raster(const DView* views, int tile, Scratch sc, int grid, int warps, cudaStream_t s);

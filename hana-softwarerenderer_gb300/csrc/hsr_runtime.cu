@@ -239,7 +239,6 @@ int Runtime::plan_build(const hsr_draw_desc* descs, int n, Plan& p) {
       bytes = align_up(bytes + sizeof(float4) * (size_t)std::max(m->nnrm, 1), 256);
       p.total_nrm += (size_t)m->nnrm;
     }
-    o.slot = bytes; bytes = align_up(bytes + sizeof(int32_t) * (size_t)std::max(m->nfaces, 1), 256);
     for (int b = 0; b < m->npos; b += 1024) p.vchunks.push_back({k, 0, b, std::min(m->npos, b + 1024)});
     if (shader_needs_wnrm(d.shader))
       for (int b = 0; b < m->nnrm; b += 1024) p.vchunks.push_back({k, 1, b, std::min(m->nnrm, b + 1024)});
@@ -253,6 +252,7 @@ int Runtime::plan_build(const hsr_draw_desc* descs, int n, Plan& p) {
   p.view_bytes = bytes;
   p.rec_cap = std::max<size_t>(cap_rec_hint, p.total_faces + p.total_faces / 4 + 1024);
   p.clip_cap = std::max<size_t>(cap_clip_hint, p.total_faces / 16 + 256);
+  p.big_cap = std::max<size_t>(cap_big_hint, p.total_faces / 64 + 256);
   p.bin_cap = std::max<size_t>(cap_bin_hint,
                                (size_t)(tuning.bin_factor * (double)(p.total_faces + p.total_tiles)) + 4096);
   return HSR_OK;
@@ -261,6 +261,7 @@ int Runtime::plan_build(const hsr_draw_desc* descs, int n, Plan& p) {
 void Plan::layout() {
   rec_cap = std::min<size_t>(rec_cap, 0xfffff000u);
   clip_cap = std::min<size_t>(clip_cap, 0xfffff000u);
+  big_cap = std::min<size_t>(big_cap, 0xfffff000u);
   bin_cap = std::min<size_t>(bin_cap, 0xfffff000u);
   nscan = scan_blocks((int)total_tiles);
   // [views | chunks | per-view vertex outputs | ctl | view_done | tile_count | tile_fill |
@@ -281,7 +282,8 @@ void Plan::layout() {
   o_toff = off; off = align_up(off + sizeof(uint32_t) * total_tiles, 256);
   o_recs = off; off = align_up(off + sizeof(RasterRec) * rec_cap, 256);
   o_pay = off; off = align_up(off + sizeof(Payload) * rec_cap, 256);
-  o_clip = off; off = align_up(off + sizeof(float) * kClipSlotFloats * clip_cap, 256);
+  o_clip = off; off = align_up(off + sizeof(int2) * clip_cap, 256);
+  o_big = off; off = align_up(off + sizeof(BigItem) * big_cap, 256);
   o_bins = off; off = align_up(off + sizeof(uint32_t) * bin_cap, 256);
   dev_bytes = off;
   stage_bytes = host_bytes + sizeof(Ctl);
@@ -295,7 +297,6 @@ void Plan::bind(char* dev_base, char* host_base) {
     v.clip = (float4*)(dev + o_vout + offs[k].clip);
     v.wpos = shader_needs_wpos(v.shader) ? (float4*)(dev + o_vout + offs[k].wpos) : nullptr;
     v.wnrm = shader_needs_wnrm(v.shader) ? (float4*)(dev + o_vout + offs[k].wnrm) : nullptr;
-    v.clip_slot = (int32_t*)(dev + o_vout + offs[k].slot);
   }
   std::memcpy(host + o_views, views.data(), sizeof(DView) * n);
   if (!vchunks.empty()) std::memcpy(host + o_vch, vchunks.data(), sizeof(Chunk) * vchunks.size());
@@ -304,7 +305,8 @@ void Plan::bind(char* dev_base, char* host_base) {
   sc.view_done = (uint32_t*)(dev + o_done);
   sc.recs = (RasterRec*)(dev + o_recs); sc.rec_cap = (uint32_t)rec_cap;
   sc.pay = (Payload*)(dev + o_pay);
-  sc.clipbuf = (float*)(dev + o_clip); sc.clip_cap = (uint32_t)clip_cap;
+  sc.clipq = (int2*)(dev + o_clip); sc.clip_cap = (uint32_t)clip_cap;
+  sc.bigq = (BigItem*)(dev + o_big); sc.big_cap = (uint32_t)big_cap;
   sc.tile_count = (uint32_t*)(dev + o_cnt);
   sc.tile_fill = (uint32_t*)(dev + o_fill);
   sc.tile_off = (uint32_t*)(dev + o_toff);
@@ -329,11 +331,13 @@ int Plan::enqueue(cudaStream_t s, int num_sms, const hsr_tuning& tu, cudaEvent_t
   if (ev && ev[2]) cudaEventRecord(ev[2], s);
   kr = launch_setup(dviews, (const Chunk*)(dev + o_sch), (int)schunks.size(), tile, sc, s);
   if (kr) return cuda_fail((cudaError_t)kr, "setup kernel");
+  kr = launch_post(dviews, tile, sc, num_sms * 2, s);
+  if (kr) return cuda_fail((cudaError_t)kr, "post kernel");
   if (ev && ev[3]) cudaEventRecord(ev[3], s);
   kr = launch_scan(sc, s);
   if (kr) return cuda_fail((cudaError_t)kr, "scan kernel");
   if (ev && ev[4]) cudaEventRecord(ev[4], s);
-  kr = launch_scatter(dviews, tile, sc, num_sms * 4, s);
+  kr = launch_scatter(dviews, tile, sc, (int)std::max<size_t>((rec_cap + 255) / 256, 1), s);
   if (kr) return cuda_fail((cudaError_t)kr, "scatter kernel");
   if (ev && ev[5]) cudaEventRecord(ev[5], s);
   kr = launch_raster(dviews, tile, sc, num_sms * tu.ctas_per_sm, tu.warps_per_cta, s);
@@ -345,12 +349,13 @@ int Plan::enqueue(cudaStream_t s, int num_sms, const hsr_tuning& tu, cudaEvent_t
 }
 
 int Plan::kernel_count() const {
-  return (vchunks.empty() ? 0 : 1) + (schunks.empty() ? 0 : 1) + (nscan > 0 ? 1 : 0) + 2;
+  return (vchunks.empty() ? 0 : 1) + (schunks.empty() ? 0 : 1) + 1 + (nscan > 0 ? 1 : 0) + 2;
 }
 
 // Grow the capacity an overflow reported; returns false if nothing overflowed.
 bool Plan::grow(const Ctl& c) {
-  if (!(c.error & (kErrRecOverflow | kErrClipOverflow | kErrBinOverflow))) return false;
+  if (!(c.error & kErrCapacity)) return false;
+  if (c.error & kErrBigOverflow) big_cap = std::max<size_t>(big_cap * 2, (size_t)c.big_count + 256);
   if (c.error & kErrRecOverflow) rec_cap = std::max<size_t>(rec_cap * 2, (size_t)c.rec_count + 1024);
   if (c.error & kErrClipOverflow) clip_cap = std::max<size_t>(clip_cap * 2, (size_t)c.clip_count + 256);
   if (c.error & kErrBinOverflow) bin_cap = std::max<size_t>(bin_cap * 2, (size_t)c.bin_total + 4096);
@@ -399,7 +404,7 @@ int Runtime::run_batch(const hsr_draw_desc* descs, int n) {
     const Ctl c = *(const Ctl*)(p.host + p.host_bytes);
     if (p.grow(c)) {
       stats.retries++;
-      cap_rec_hint = p.rec_cap; cap_clip_hint = p.clip_cap; cap_bin_hint = p.bin_cap;
+      cap_rec_hint = p.rec_cap; cap_clip_hint = p.clip_cap; cap_bin_hint = p.bin_cap; cap_big_hint = p.big_cap;
       continue;
     }
     if (c.error & (kErrWaitTimeout | kErrScanTimeout))
@@ -715,9 +720,8 @@ int hsr_get_tuning(hsr_tuning* out) {
 int hsr_set_tuning(const hsr_tuning* in) {
   RT_OR_FAIL();
   if (!in) return fail(HSR_ERR_INVALID_ARG, "set_tuning: null");
-  if (in->tile != 8 && in->tile != 16 && in->tile != 32) return fail(HSR_ERR_INVALID_ARG, "set_tuning: tile must be 8, 16 or 32");
+  if (in->tile != 8 && in->tile != 16) return fail(HSR_ERR_INVALID_ARG, "set_tuning: tile must be 8 or 16");
   if (in->warps_per_cta != 4 && in->warps_per_cta != 8) return fail(HSR_ERR_INVALID_ARG, "set_tuning: warps_per_cta must be 4 or 8");
-  if (in->tile == 32 && in->warps_per_cta != 4) return fail(HSR_ERR_INVALID_ARG, "set_tuning: tile 32 needs 4 warps per CTA");
   if (in->ctas_per_sm < 1 || in->ctas_per_sm > 16) return fail(HSR_ERR_INVALID_ARG, "set_tuning: ctas_per_sm in [1,16]");
   if (!(in->bin_factor >= 0.5f && in->bin_factor <= 64.f)) return fail(HSR_ERR_INVALID_ARG, "set_tuning: bin_factor in [0.5,64]");
   g_rt->tuning = *in;

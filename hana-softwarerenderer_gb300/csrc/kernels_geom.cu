@@ -209,58 +209,41 @@ __device__ void append_small(bool valid, const RasterRec& r, const Payload& pl, 
   }
 }
 
-// Emit the records of a warp.  A triangle whose bounding box touches more than
-// kMaxRecordTiles tiles becomes sub-records over blocks of kSubTilesX x kSubTilesY tiles:
-// same triangle constants and seq, pixel range clipped to the block, payload shared with
-// the first sub-record.  The union of the sub-ranges is the triangle's pixel range, so
-// every covered pixel is still tested exactly once.
-__device__ void commit(bool valid, const RasterRec& r, const Payload& pl, const DView& v, int T,
-                       const Scratch& sc) {
+// Expand one triangle whose bounding box touches more than kMaxRecordTiles tiles into
+// sub-records over blocks of kSubTilesX x kSubTilesY tiles: same triangle constants and
+// seq, pixel range clipped to the block, one payload shared by all of them (stored at the
+// first sub-record's slot).  The union of the sub-ranges is the triangle's pixel range, so
+// every pixel is tested exactly once.  All 32 lanes call this with the same `b`;
+// `copy_payload(dst)` stores the payload (called by lane 0).
+template <class CopyPayload>
+__device__ void expand_big(const RasterRec& b, const DView& v, int T, const Scratch& sc, CopyPayload copy_payload) {
   const int lane = threadIdx.x & 31;
-  const int nf4 = payload_f4(v.shader);
-  int tx0 = 0, ty0 = 0, ntw = 1, nt = 0;
-  if (valid) rec_tiles(r, T, tx0, ty0, ntw, nt);
-  const bool big = valid && nt > kMaxRecordTiles;
-  append_small(valid && !big, r, pl, nf4, v, T, sc);
-
-  unsigned bm = __ballot_sync(kFull, big);
-  while (bm) {
-    const int l = __ffs(bm) - 1;
-    bm &= bm - 1;
-    RasterRec b;
-    {
-      const uint32_t* src = reinterpret_cast<const uint32_t*>(&r);
-      uint32_t* dst = reinterpret_cast<uint32_t*>(&b);
-#pragma unroll
-      for (int q = 0; q < 16; q++) dst[q] = __shfl_sync(kFull, src[q], l);
-    }
-    const int btx0 = __shfl_sync(kFull, tx0, l), bty0 = __shfl_sync(kFull, ty0, l);
-    const int bntw = __shfl_sync(kFull, ntw, l), bnt = __shfl_sync(kFull, nt, l);
-    const int bnth = bnt / bntw;
-    const int nbx = (bntw + kSubTilesX - 1) / kSubTilesX, nby = (bnth + kSubTilesY - 1) / kSubTilesY;
-    const int nsub = nbx * nby;
-    uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(&sc.ctl->rec_count, (uint32_t)nsub);
-    base = __shfl_sync(kFull, base, 0);
-    if ((uint64_t)base + (uint64_t)nsub > (uint64_t)sc.rec_cap) {
-      if (lane == 0) atomicOr(&sc.ctl->error, kErrRecOverflow);
-      continue;
-    }
-    if (lane == l) store_payload(&sc.pay[base], pl, nf4);
-    const int x0 = (int)(b.xr & 0xffffu), x1 = (int)(b.xr >> 16);
-    const int y0 = (int)(b.yr & 0xffffu), y1 = (int)(b.yr >> 16);
-    for (int sidx = lane; sidx < nsub; sidx += 32) {
-      const int bx = sidx % nbx, by = sidx / nbx;
-      const int stx0 = btx0 + bx * kSubTilesX, stx1 = min(btx0 + bntw - 1, stx0 + kSubTilesX - 1);
-      const int sty0 = bty0 + by * kSubTilesY, sty1 = min(bty0 + bnth - 1, sty0 + kSubTilesY - 1);
-      RasterRec w = b;
-      w.xr = (uint32_t)max(x0, stx0 * T) | ((uint32_t)min(x1, stx1 * T + T - 1) << 16);
-      w.yr = (uint32_t)max(y0, sty0 * T) | ((uint32_t)min(y1, sty1 * T + T - 1) << 16);
-      w.pad = base;
-      store_rec(&sc.recs[base + (uint32_t)sidx], w);
-      for (int ty = sty0; ty <= sty1; ty++)
-        for (int tx = stx0; tx <= stx1; tx++) atomicAdd(&sc.tile_count[v.tile_base + ty * v.tiles_x + tx], 1u);
-    }
+  int tx0, ty0, ntw, nt;
+  rec_tiles(b, T, tx0, ty0, ntw, nt);
+  const int nth = nt / ntw;
+  const int nbx = (ntw + kSubTilesX - 1) / kSubTilesX, nby = (nth + kSubTilesY - 1) / kSubTilesY;
+  const int nsub = nbx * nby;
+  uint32_t base = 0;
+  if (lane == 0) base = atomicAdd(&sc.ctl->rec_count, (uint32_t)nsub);
+  base = __shfl_sync(kFull, base, 0);
+  if ((uint64_t)base + (uint64_t)nsub > (uint64_t)sc.rec_cap) {
+    if (lane == 0) atomicOr(&sc.ctl->error, kErrRecOverflow);
+    return;
+  }
+  if (lane == 0) copy_payload(&sc.pay[base]);
+  const int x0 = (int)(b.xr & 0xffffu), x1 = (int)(b.xr >> 16);
+  const int y0 = (int)(b.yr & 0xffffu), y1 = (int)(b.yr >> 16);
+  for (int sidx = lane; sidx < nsub; sidx += 32) {
+    const int bx = sidx % nbx, by = sidx / nbx;
+    const int stx0 = tx0 + bx * kSubTilesX, stx1 = min(tx0 + ntw - 1, stx0 + kSubTilesX - 1);
+    const int sty0 = ty0 + by * kSubTilesY, sty1 = min(ty0 + nth - 1, sty0 + kSubTilesY - 1);
+    RasterRec w = b;
+    w.xr = (uint32_t)max(x0, stx0 * T) | ((uint32_t)min(x1, stx1 * T + T - 1) << 16);
+    w.yr = (uint32_t)max(y0, sty0 * T) | ((uint32_t)min(y1, sty1 * T + T - 1) << 16);
+    w.pad = base;
+    store_rec(&sc.recs[base + (uint32_t)sidx], w);
+    for (int ty = sty0; ty <= sty1; ty++)
+      for (int tx = stx0; tx <= stx1; tx++) atomicAdd(&sc.tile_count[v.tile_base + ty * v.tiles_x + tx], 1u);
   }
 }
 
@@ -297,13 +280,22 @@ __device__ __forceinline__ bool vertex_visible(float4 c) {  // is_vertex_visible
 constexpr int kSetupThreads = 256;
 constexpr int kPolyStride = kVaryings;  // floats per polygon vertex in shared memory
 
+// Warp-aggregated append of one item per participating lane; returns the slot or ~0u.
+__device__ __forceinline__ uint32_t warp_append(bool want, uint32_t* counter) {
+  const int lane = threadIdx.x & 31;
+  const unsigned m = __ballot_sync(kFull, want);
+  if (!m) return ~0u;
+  const int leader = __ffs(m) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
+  base = __shfl_sync(kFull, base, leader);
+  return want ? base + (uint32_t)__popc(m & ((1u << lane) - 1u)) : ~0u;
+}
+
 __global__ void __launch_bounds__(kSetupThreads) k_setup(const DView* __restrict__ views,
                                                          const Chunk* __restrict__ chunks, int T, Scratch sc) {
-  // per warp: two ping-pong polygons of up to 16 vertices x 13 varyings
-  __shared__ float poly[kSetupThreads / 32][2][16 * kPolyStride];
   const Chunk ch = chunks[blockIdx.x];
   const DView& v = views[ch.view];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int f = ch.begin + (int)threadIdx.x;
   const bool active = f < ch.end;
 
@@ -341,85 +333,144 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const DView* __restrict
       needs_clip = true;
     }
   }
-  commit(valid, r, pl, v, T, sc);
+  int tx0, ty0, ntw, nt = 0;
+  if (valid) rec_tiles(r, T, tx0, ty0, ntw, nt);
+  const bool big = valid && nt > kMaxRecordTiles;
+  append_small(valid && !big, r, pl, payload_f4(v.shader), v, T, sc);
 
-  // ---- homogeneous clipping, one face at a time per warp (graphics.cpp:73-161) ---------
-  unsigned cm = __ballot_sync(kFull, needs_clip);
-  while (cm) {
-    const int l = __ffs(cm) - 1;
-    cm &= cm - 1;
-    const int face = __shfl_sync(kFull, f, l);
-    float* A = poly[warp][0];
-    float* B = poly[warp][1];
-    if (lane < 3) {
-      const int4 iv = __ldg(&v.fv[face]), it = __ldg(&v.fvt[face]), in = __ldg(&v.fvn[face]);
-      const int pi = lane == 0 ? iv.x : (lane == 1 ? iv.y : iv.z);
-      const int ti = lane == 0 ? it.x : (lane == 1 ? it.y : it.z);
-      const int ni = lane == 0 ? in.x : (lane == 1 ? in.y : in.z);
-      float* o = A + lane * kPolyStride;
-      const float4 c = v.clip[pi];
-      o[0] = c.x; o[1] = c.y; o[2] = c.z; o[3] = c.w;
-      float4 wp = v.wpos ? v.wpos[pi] : make_float4(0.f, 0.f, 0.f, 0.f);
-      float4 wn = v.wnrm ? v.wnrm[ni] : make_float4(0.f, 0.f, 0.f, 0.f);
-      float2 t = v.uv ? __ldg(&v.uv[ti]) : make_float2(0.f, 0.f);
-      o[4] = wp.x; o[5] = wp.y; o[6] = wp.z;
-      o[7] = wn.x; o[8] = wn.y; o[9] = wn.z;
-      o[10] = t.x; o[11] = t.y; o[12] = wn.w;
+  // huge triangles and faces that need the clipper are queued for k_post, which spreads
+  // them over the whole GPU instead of leaving one warp to work through a cluster of them
+  const uint32_t bslot = warp_append(big, &sc.ctl->big_count);
+  if (big) {
+    if (bslot < sc.big_cap) {
+      store_rec(&sc.bigq[bslot].rec, r);
+      store_payload(&sc.bigq[bslot].pay, pl, payload_f4(v.shader));
+    } else {
+      atomicOr(&sc.ctl->error, kErrBigOverflow);
     }
-    __syncwarp();
-    int n = 3;
-    float* src = A;
-    float* dst = B;
-    for (int plane = PW; plane <= NZ && n >= 3; plane++) {
-      int m = 0;
-      for (int i = 0; i < n; i++) {
-        const float* prev = src + ((i - 1 + n) % n) * kPolyStride;
-        const float* curr = src + i * kPolyStride;
-        const bool pin = inside_plane(prev, plane), cin = inside_plane(curr, plane);
-        if (pin != cin) {
-          const float t = intersect_ratio(prev, curr, plane);
-          if (lane < kVaryings) dst[m * kPolyStride + lane] = fa(prev[lane], fm(fs(curr[lane], prev[lane]), t));
-          m++;
-        }
-        if (cin) {
-          if (lane < kVaryings) dst[m * kPolyStride + lane] = curr[lane];
-          m++;
-        }
-      }
-      __syncwarp();
-      n = m;
-      float* tmp = src; src = dst; dst = tmp;
-    }
-    bool cvalid = false;
-    RasterRec cr;
-    Payload cpl;
-    if (n >= 3) {
-      uint32_t slot = 0;
-      if (lane == 0) slot = atomicAdd(&sc.ctl->clip_count, 1u);
-      slot = __shfl_sync(kFull, slot, 0);
-      if (slot < sc.clip_cap) {
-        float* out = sc.clipbuf + (size_t)slot * kClipSlotFloats;
-        if (lane == 0) {
-          out[0] = __int_as_float(n);
-          v.clip_slot[face] = (int32_t)slot;
-        }
-        for (int k = lane; k < n * kVaryings; k += 32) out[4 + k] = src[k];
-        if (lane < n - 2) {
-          const float* p0 = src;
-          const float* p1 = src + (lane + 1) * kPolyStride;
-          const float* p2 = src + (lane + 2) * kPolyStride;
-          cvalid = build_rec(v, make_float4(p0[0], p0[1], p0[2], p0[3]), make_float4(p1[0], p1[1], p1[2], p1[3]),
-                             make_float4(p2[0], p2[1], p2[2], p2[3]),
-                             ((uint32_t)face << 4) | ((uint32_t)lane << 1) | 1u, (uint32_t)ch.view, cr);
-          if (cvalid) make_payload(v.shader, p0, p1, p2, cpl);
-        }
-      } else if (lane == 0) {
-        atomicOr(&sc.ctl->error, kErrClipOverflow);
-      }
-    }
-    commit(cvalid, cr, cpl, v, T, sc);
-    __syncwarp();
   }
+  const uint32_t cslot = warp_append(needs_clip, &sc.ctl->clip_count);
+  if (needs_clip) {
+    if (cslot < sc.clip_cap) sc.clipq[cslot] = make_int2(ch.view, f);
+    else atomicOr(&sc.ctl->error, kErrClipOverflow);
+  }
+}
+
+// Homogeneous clipping of one face by one warp (graphics.cpp:73-161): lane k carries
+// varying k of the polygon through Sutherland-Hodgman while every lane evaluates the plane
+// tests on the clip coordinates; lanes j < n-2 then build the fan triangles (:394-405).
+__device__ void clip_face(const DView& v, int view, int face, int T, const Scratch& sc, float* A, float* B) {
+  const int lane = threadIdx.x & 31;
+  if (lane < 3) {
+    const int4 iv = __ldg(&v.fv[face]), it = __ldg(&v.fvt[face]), in = __ldg(&v.fvn[face]);
+    const int pi = lane == 0 ? iv.x : (lane == 1 ? iv.y : iv.z);
+    const int ti = lane == 0 ? it.x : (lane == 1 ? it.y : it.z);
+    const int ni = lane == 0 ? in.x : (lane == 1 ? in.y : in.z);
+    float* o = A + lane * kPolyStride;
+    const float4 c = v.clip[pi];
+    o[0] = c.x; o[1] = c.y; o[2] = c.z; o[3] = c.w;
+    const float4 wp = v.wpos ? v.wpos[pi] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 wn = v.wnrm ? v.wnrm[ni] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2 t = v.uv ? __ldg(&v.uv[ti]) : make_float2(0.f, 0.f);
+    o[4] = wp.x; o[5] = wp.y; o[6] = wp.z;
+    o[7] = wn.x; o[8] = wn.y; o[9] = wn.z;
+    o[10] = t.x; o[11] = t.y; o[12] = wn.w;
+  }
+  __syncwarp();
+  int n = 3;
+  float* src = A;
+  float* dst = B;
+  for (int plane = PW; plane <= NZ && n >= 3; plane++) {
+    int m = 0;
+    for (int i = 0; i < n; i++) {
+      const float* prev = src + ((i - 1 + n) % n) * kPolyStride;
+      const float* curr = src + i * kPolyStride;
+      const bool pin = inside_plane(prev, plane), cin = inside_plane(curr, plane);
+      if (pin != cin) {
+        const float t = intersect_ratio(prev, curr, plane);
+        if (lane < kVaryings) dst[m * kPolyStride + lane] = fa(prev[lane], fm(fs(curr[lane], prev[lane]), t));
+        m++;
+      }
+      if (cin) {
+        if (lane < kVaryings) dst[m * kPolyStride + lane] = curr[lane];
+        m++;
+      }
+    }
+    __syncwarp();
+    n = m;
+    float* tmp = src; src = dst; dst = tmp;
+  }
+  bool valid = false;
+  RasterRec r;
+  Payload pl;
+  if (n >= 3 && lane < n - 2) {
+    const float* p0 = src;
+    const float* p1 = src + (lane + 1) * kPolyStride;
+    const float* p2 = src + (lane + 2) * kPolyStride;
+    valid = build_rec(v, make_float4(p0[0], p0[1], p0[2], p0[3]), make_float4(p1[0], p1[1], p1[2], p1[3]),
+                      make_float4(p2[0], p2[1], p2[2], p2[3]), ((uint32_t)face << 4) | ((uint32_t)lane << 1) | 1u,
+                      (uint32_t)view, r);
+    if (valid) make_payload(v.shader, p0, p1, p2, pl);
+  }
+  int tx0, ty0, ntw, nt = 0;
+  if (valid) rec_tiles(r, T, tx0, ty0, ntw, nt);
+  const bool big = valid && nt > kMaxRecordTiles;
+  const int nf4 = payload_f4(v.shader);
+  append_small(valid && !big, r, pl, nf4, v, T, sc);
+  unsigned bm = __ballot_sync(kFull, big);
+  while (bm) {
+    const int l = __ffs(bm) - 1;
+    bm &= bm - 1;
+    RasterRec b;
+    const uint32_t* srcw = reinterpret_cast<const uint32_t*>(&r);
+    uint32_t* dstw = reinterpret_cast<uint32_t*>(&b);
+#pragma unroll
+    for (int q = 0; q < 16; q++) dstw[q] = __shfl_sync(kFull, srcw[q], l);
+    // the payload lives in lane l's registers: hand it over through the lanes' shuffle
+    float pw[kPayloadFloats];
+#pragma unroll
+    for (int q = 0; q < kPayloadFloats; q++) pw[q] = __shfl_sync(kFull, pl.f[q], l);
+    expand_big(b, v, T, sc, [&](Payload* dstp) {
+      Payload tmp;
+#pragma unroll
+      for (int q = 0; q < kPayloadFloats; q++) tmp.f[q] = pw[q];
+      store_payload(dstp, tmp, nf4);
+    });
+  }
+  __syncwarp();
+}
+
+constexpr int kPostThreads = 256;
+
+// Drains the clip queue and the big-triangle queue of k_setup, one warp per item.
+__global__ void __launch_bounds__(kPostThreads) k_post(const DView* __restrict__ views, int T, Scratch sc) {
+  __shared__ float poly[kPostThreads / 32][2][16 * kPolyStride];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (sc.ctl->error & kErrCapacity) return;
+  const uint32_t nclip = min(sc.ctl->clip_count, sc.clip_cap);
+  const uint32_t nbig = min(sc.ctl->big_count, sc.big_cap);
+  const uint32_t total = nclip + nbig;
+  for (;;) {
+    uint32_t item = 0;
+    if (lane == 0) item = atomicAdd(&sc.ctl->post_next, 1u);
+    item = __shfl_sync(kFull, item, 0);
+    if (item >= total) break;
+    if (item < nclip) {
+      const int2 vf = sc.clipq[item];
+      clip_face(views[vf.x], vf.x, vf.y, T, sc, poly[warp][0], poly[warp][1]);
+    } else {
+      const BigItem& bi = sc.bigq[item - nclip];
+      const RasterRec b = bi.rec;
+      const DView& v = views[b.view];
+      const int nf4 = payload_f4(v.shader);
+      expand_big(b, v, T, sc, [&](Payload* dstp) { store_payload(dstp, bi.pay, nf4); });
+    }
+  }
+}
+
+int launch_post(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s) {
+  k_post<<<grid, kPostThreads, 0, s>>>(views, tile, sc);
+  return (int)cudaGetLastError();
 }
 
 int launch_setup(const DView* views, const Chunk* chunks, int nchunks, int tile, Scratch sc, cudaStream_t s) {

@@ -6,9 +6,9 @@
 // fragment of minimum depth, and among equal minima the LAST submitted one; a previous
 // buffer depth equal to that minimum loses.  Fragment depths are never -0 or NaN
 // (interpolate_depth starts from +0), so the order-independent rule
-//     new wins  <=>  z < best_z  ||  (z == best_z && seq > best_seq)
-// with best initialised from the buffer (seq "-1"; NaN buffer depth -> +inf) reproduces
-// the loop exactly, whatever order the tile lists hold.  All shaders return
+//     min over (depth, later-submitted)
+// with the buffer's depth as the weakest entry reproduces the loop exactly, whatever
+// order the tile lists hold.  All shaders return
 // `discard = false` and have no side effects (IShader.cpp:14,38,56,76,108,161,179), so
 // shading only the winner equals shading every passing fragment in order.
 //
@@ -28,12 +28,6 @@ namespace hsr {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr long kWaitLimit = 1L << 23;  // ~1-2 s of polling before a dependency wait gives up
-
-__device__ __forceinline__ float canon_depth(float d) {
-  // the stored depth a fragment is compared with: NaN admits every fragment (z > NaN is
-  // false), which an ordered compare gets from +inf
-  return d != d ? __int_as_float(0x7f800000) : d;
-}
 
 // interpolate_varyings (graphics.cpp:205-220) for one float
 __device__ __forceinline__ float interp(float s0, float s1, float s2, float w0, float w1, float w2, float nrm) {
@@ -106,17 +100,49 @@ __device__ __forceinline__ void wait_view(const Scratch& sc, const DView* views,
   __threadfence();
 }
 
+// Ordered bits of a float: unsigned order equals float order (-inf < ... < -0 < +0 < ... < +inf).
+__device__ __forceinline__ uint32_t ord_bits(float f) {
+  const uint32_t b = __float_as_uint(f);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float from_ord(uint32_t o) {
+  return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
+}
+// Key of the depth already in the buffer: it loses every tie (low word above any fragment's),
+// -0 compares equal to +0 as `frag_depth > depth` does, NaN admits every fragment.
+__device__ __forceinline__ unsigned long long buffer_key(float d) {
+  if (d == 0.f) d = 0.f;
+  if (d != d) d = __int_as_float(0x7f800000);
+  return ((unsigned long long)ord_bits(d) << 32) | 0xffffffffull;
+}
+
+// q / d for q < 1024 and 1 <= d <= 32 by multiply-shift: ceil(65536 / d).
+__constant__ uint32_t kDivMagic[33] = {0,     65536, 32768, 21846, 16384, 13108, 10923, 9363, 8192, 7282, 6554,
+                                       5958,  5462,  5042,  4682,  4370,  4096,  3856,  3641, 3450, 3277, 3121,
+                                       2979,  2850,  2731,  2622,  2521,  2428,  2341,  2260, 2185, 2115, 2048};
+
+// One warp per screen tile.  For each batch of 32 records of the tile list, every record's
+// bounding-box pixels inside the tile form a run of candidates; the runs are laid end to
+// end (warp prefix sum) and the lanes walk the candidates 32 at a time, so the work is
+// proportional to the pixels the triangles can touch rather than to records x 32 lanes.
+// A covered candidate resolves visibility with a 64-bit atomicMin on
+//     (ordered depth << 32) | (0xfffffffe - seq)
+// in shared memory: smallest depth first, and among equal depths the later submission.
+// The lane whose key is still the minimum after the warp's atomics records its record as
+// the pixel's winner (two lanes of one step never hold the same key: one triangle covers a
+// pixel once).  Shading then runs once per pixel with a winner.
 template <int T, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32, T == 32 ? 2 : 32 / WARPS) k_raster(const DView* __restrict__ views, Scratch sc) {
-  constexpr int RP = 32 / T;        // rows covered by one pass of the warp
-  constexpr int PPL = T * T / 32;   // pixels per lane
+__global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* __restrict__ views, Scratch sc) {
+  constexpr int NPIX = T * T;
+  constexpr int PPL = NPIX / 32;
+  __shared__ unsigned long long skey[WARPS][NPIX];
+  __shared__ uint32_t swin[WARPS][NPIX];
   __shared__ RasterRec srec[WARPS][32];
   __shared__ uint32_t sidx[WARPS][32];
-  __shared__ uint32_t swin[WARPS][T * T];
-  __shared__ float sz[WARPS][T * T];
+  __shared__ uint32_t soff[WARPS][32];
+  __shared__ uint32_t sbox[WARPS][32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (sc.ctl->error & (kErrBinOverflow | kErrRecOverflow | kErrClipOverflow | kErrScanTimeout)) return;
-  const int col = lane % T, row = lane / T;
+  if (sc.ctl->error & kErrCapacity) return;
   const uint32_t nrec = min(sc.ctl->rec_count, sc.rec_cap);
 
   for (;;) {
@@ -133,16 +159,16 @@ __global__ void __launch_bounds__(WARPS * 32, T == 32 ? 2 : 32 / WARPS) k_raster
     __syncwarp();
     const int lt = (int)t - v.tile_base;
     const int tx = lt % v.tiles_x, ty = lt / v.tiles_x;
-    const int x = tx * T + col;
-    const int ybase = ty * T + row;
+    const int ox = tx * T, oy = ty * T;
     const bool clear = (v.flags & HSR_DRAW_CLEAR) != 0u;
     const uint32_t n = sc.tile_count[t];
 
     if (n == 0) {
       if (clear) {
 #pragma unroll
-        for (int k = 0; k < PPL; k++) {
-          const int y = ybase + k * RP;
+        for (int q = 0; q < PPL; q++) {
+          const int p = lane + 32 * q;
+          const int x = ox + p % T, y = oy + p / T;
           if (x < v.W && y < v.H) {
             const size_t idx = (size_t)y * v.W + x;
             v.color[idx] = v.clear_rgba;
@@ -152,96 +178,112 @@ __global__ void __launch_bounds__(WARPS * 32, T == 32 ? 2 : 32 / WARPS) k_raster
         }
       }
     } else {
-      float cz[PPL];
-      uint32_t cs[PPL], cw[PPL];
 #pragma unroll
-      for (int k = 0; k < PPL; k++) {
-        const int y = ybase + k * RP;
+      for (int q = 0; q < PPL; q++) {
+        const int p = lane + 32 * q;
+        const int x = ox + p % T, y = oy + p / T;
         float d = v.clear_depth;
         if (!clear && x < v.W && y < v.H) d = __ldcg(&v.depth[(size_t)y * v.W + x]);
-        cz[k] = canon_depth(d);
-        cs[k] = 0u;
-        cw[k] = 0u;
+        skey[warp][p] = buffer_key(d);
+        swin[warp][p] = 0xffffffffu;
       }
       const uint32_t off = sc.tile_off[t];
-      const float pxf = (float)x;
       for (uint32_t b = 0; b < n; b += 32) {
         const uint32_t cnt = min(32u, n - b);
+        uint32_t c = 0;
+        __syncwarp();
         if ((uint32_t)lane < cnt) {
           const uint32_t ri = sc.bins[off + b + (uint32_t)lane];
           RasterRec rr;
           if (ri < nrec) {
             rr = sc.recs[ri];
-          } else {        // never produced by a consistent bin pass; covers no pixel
-            rr.xr = 1u;
-            rr.yr = 1u;
-            rr.seq = 0u;
-            rr.flags = 0u;
-            rr.pad = 0u;
+          } else {  // never produced by a consistent bin pass: covers nothing
+            rr.xr = 1u; rr.yr = 1u; rr.seq = 0u; rr.flags = 0u; rr.pad = 0u;
+          }
+          const int lx0 = max((int)(rr.xr & 0xffffu) - ox, 0), lx1 = min((int)(rr.xr >> 16) - ox, T - 1);
+          const int ly0 = max((int)(rr.yr & 0xffffu) - oy, 0), ly1 = min((int)(rr.yr >> 16) - oy, T - 1);
+          if (lx0 <= lx1 && ly0 <= ly1) {
+            c = (uint32_t)((lx1 - lx0 + 1) * (ly1 - ly0 + 1));
+            sbox[warp][lane] = (uint32_t)lx0 | ((uint32_t)ly0 << 8) | ((uint32_t)(lx1 - lx0 + 1) << 16);
           }
           srec[warp][lane] = rr;
           sidx[warp][lane] = ri;
         }
-        __syncwarp();
-        for (uint32_t j = 0; j < cnt; j++) {
-          const RasterRec& r = srec[warp][j];
-          const int x0 = (int)(r.xr & 0xffffu), x1 = (int)(r.xr >> 16);
-          const int y0 = (int)(r.yr & 0xffffu), y1 = (int)(r.yr >> 16);
-          const int r0 = max(y0 - ty * T, 0), r1 = min(y1 - ty * T, T - 1);
-          const int k0 = r0 / RP, k1 = r1 / RP;
-          const bool xin = x >= x0 && x <= x1;
-          const uint32_t seqp1 = r.seq + 1u;
-          const bool exact = (r.flags & kRecExact) != 0u;
+        uint32_t incl = c;
 #pragma unroll
-          for (int k = 0; k < PPL; k++) {
-            if (k < k0 || k > k1) continue;
-            const int y = ybase + k * RP;
-            if (!xin || y < y0 || y > y1) continue;
-            const float pyf = (float)y;
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t y = __shfl_up_sync(kFull, incl, o);
+          if (lane >= o) incl += y;
+        }
+        const uint32_t W = __shfl_sync(kFull, incl, 31);
+        soff[warp][lane] = incl - c;
+        __syncwarp();
+        for (uint32_t base = 0; base < W; base += 32) {
+          const uint32_t i = base + (uint32_t)lane;
+          bool covered = false;
+          unsigned long long key = 0ull, old = 0ull;
+          int p = 0, j = 0;
+          if (i < W) {
+            // record j owning candidate i: the last j with soff[j] <= i (empty runs never win)
+            int lo = 0, hi = (int)cnt - 1;
+#pragma unroll
+            for (int s = 0; s < 5; s++) {
+              const int mid = (lo + hi + 1) >> 1;
+              if (lo < hi) {
+                if (soff[warp][mid] <= i) lo = mid; else hi = mid - 1;
+              }
+            }
+            j = lo;
+            const uint32_t q = i - soff[warp][j];
+            const uint32_t box = sbox[warp][j];
+            const uint32_t lw = box >> 16;
+            const uint32_t qy = (q * kDivMagic[lw]) >> 16;
+            const int lx = (int)(box & 255u) + (int)(q - qy * lw);
+            const int ly = (int)((box >> 8) & 255u) + (int)qy;
+            p = ly * T + lx;
+            const RasterRec& r = srec[warp][j];
+            const float pxf = (float)(ox + lx), pyf = (float)(oy + ly);
+            // barycentric() at integer P (graphics.cpp:222-233)
             const float dx = fs(r.ax, pxf), dy = fs(r.ay, pyf);
             const float ux = fs(fm(r.e1x, dy), fm(dx, r.e1y));
             const float uy = fs(fm(dx, r.e2y), fm(r.e2x, dy));
-            const float s = fa(ux, uy);
-            bool cov;
+            const float su = fa(ux, uy);
             float b0, b1, b2;
-            if (!exact) {
-              cov = (r.uz < 0.f) ? (s >= r.uz && uy <= 0.f && ux <= 0.f) : (s <= r.uz && uy >= 0.f && ux >= 0.f);
-              if (!cov) continue;
-              b0 = fs(1.f, fd(s, r.uz));
-              b1 = fd(uy, r.uz);
-              b2 = fd(ux, r.uz);
+            if (!(r.flags & kRecExact)) {
+              covered = (r.uz < 0.f) ? (su >= r.uz && uy <= 0.f && ux <= 0.f) : (su <= r.uz && uy >= 0.f && ux >= 0.f);
+              if (covered) {
+                b0 = fs(1.f, fd(su, r.uz));
+                b1 = fd(uy, r.uz);
+                b2 = fd(ux, r.uz);
+              }
             } else {
-              b0 = fs(1.f, fd(s, r.uz));
+              b0 = fs(1.f, fd(su, r.uz));
               b1 = fd(uy, r.uz);
               b2 = fd(ux, r.uz);
-              if (b0 < 0.f || b1 < 0.f || b2 < 0.f) continue;
+              covered = !(b0 < 0.f || b1 < 0.f || b2 < 0.f);
             }
-            // interpolate_depth (graphics.cpp:186-194)
-            const float z = fa(fa(fa(0.f, fm(r.d2, b2)), fm(r.d1, b1)), fm(r.d0, b0));
-            if (z < cz[k] || (z == cz[k] && seqp1 > cs[k])) {
-              cz[k] = z;
-              cs[k] = seqp1;
-              cw[k] = sidx[warp][j];
+            if (covered) {
+              // interpolate_depth (graphics.cpp:186-194)
+              const float z = fa(fa(fa(0.f, fm(r.d2, b2)), fm(r.d1, b1)), fm(r.d0, b0));
+              key = ((unsigned long long)ord_bits(z) << 32) | (unsigned long long)(0xfffffffeu - r.seq);
+              old = atomicMin(&skey[warp][p], key);
             }
           }
+          __syncwarp();
+          if (covered && old > key && skey[warp][p] == key) swin[warp][p] = sidx[warp][j];
+          __syncwarp();
         }
-        __syncwarp();
-      }
-      // hand the winners to shared memory so the (large) shading code is not unrolled
-#pragma unroll
-      for (int k = 0; k < PPL; k++) {
-        swin[warp][k * 32 + lane] = cs[k] ? cw[k] : 0xffffffffu;
-        sz[warp][k * 32 + lane] = cz[k];
       }
       __syncwarp();
       uint32_t shaded = 0;
       const int nf4 = payload_f4_r(v.shader);
 #pragma unroll 1
-      for (int k = 0; k < PPL; k++) {
-        const int y = ybase + k * RP;
+      for (int q = 0; q < PPL; q++) {
+        const int p = lane + 32 * q;
+        const int x = ox + p % T, y = oy + p / T;
         if (x >= v.W || y >= v.H) continue;
         const size_t idx = (size_t)y * v.W + x;
-        const uint32_t w = swin[warp][k * 32 + lane];
+        const uint32_t w = swin[warp][p];
         if (w != 0xffffffffu) {
           shaded++;
           // the payload index equals the record index except for sub-records of a split
@@ -252,18 +294,18 @@ __global__ void __launch_bounds__(WARPS * 32, T == 32 ? 2 : 32 / WARPS) k_raster
             float4* dst = reinterpret_cast<float4*>(P);
             const float4* src = reinterpret_cast<const float4*>(&sc.pay[w]);
 #pragma unroll
-            for (int q = 0; q < kPayloadFloats / 4; q++)
-              dst[q] = q < nf4 ? src[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int k = 0; k < kPayloadFloats / 4; k++)
+              dst[k] = k < nf4 ? src[k] : make_float4(0.f, 0.f, 0.f, 0.f);
             if (r.pad != w) {
               src = reinterpret_cast<const float4*>(&sc.pay[r.pad]);
 #pragma unroll
-              for (int q = 0; q < kPayloadFloats / 4; q++)
-                dst[q] = q < nf4 ? src[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+              for (int k = 0; k < kPayloadFloats / 4; k++)
+                dst[k] = k < nf4 ? src[k] : make_float4(0.f, 0.f, 0.f, 0.f);
             }
           }
           const uint32_t alpha = clear ? v.clear_rgba : __ldcg(&v.color[idx]);
           v.color[idx] = shade_pixel(v, r, P, x, y, alpha);
-          v.depth[idx] = sz[warp][k * 32 + lane];
+          v.depth[idx] = from_ord((uint32_t)(skey[warp][p] >> 32));
           if (v.prim) v.prim[idx] = v.prim_base + (r.seq >> 4) + 1u;
         } else if (clear) {
           v.color[idx] = v.clear_rgba;
@@ -273,7 +315,6 @@ __global__ void __launch_bounds__(WARPS * 32, T == 32 ? 2 : 32 / WARPS) k_raster
       }
       shaded = __reduce_add_sync(kFull, shaded);
       if (lane == 0 && shaded) atomicAdd(&sc.ctl->shaded_px, (unsigned long long)shaded);
-      __syncwarp();
     }
     if (v.has_dependents) {
       // publish this tile's writes before counting it done (a later view reads them)
@@ -281,6 +322,7 @@ __global__ void __launch_bounds__(WARPS * 32, T == 32 ? 2 : 32 / WARPS) k_raster
       __syncwarp();
       if (lane == 0) atomicAdd(&sc.view_done[vi], 1u);
     }
+    __syncwarp();
   }
 }
 
@@ -295,7 +337,6 @@ int launch_raster(const DView* views, int tile, Scratch sc, int grid, int warps,
   switch (tile) {
     case 8: return warps == 4 ? launch_t<8, 4>(views, sc, grid, s) : launch_t<8, 8>(views, sc, grid, s);
     case 16: return warps == 4 ? launch_t<16, 4>(views, sc, grid, s) : launch_t<16, 8>(views, sc, grid, s);
-    case 32: return warps == 4 ? launch_t<32, 4>(views, sc, grid, s) : (int)cudaErrorInvalidValue;
     default: return (int)cudaErrorInvalidValue;
   }
 }

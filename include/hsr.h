@@ -159,7 +159,7 @@ HSR_API int hsr_synchronize(void);
 
 /* ---- tuning ------------------------------------------------------------------------- */
 typedef struct hsr_tuning {
-  int32_t tile;           /* raster tile edge in pixels: 8, 16 or 32                */
+  int32_t tile;           /* raster tile edge in pixels: 8 or 16                    */
   int32_t ctas_per_sm;    /* persistent raster CTAs per SM                          */
   int32_t warps_per_cta;  /* warps per raster CTA (one warp owns one tile)          */
   float bin_factor;       /* bin capacity = bin_factor * (faces + tiles) pairs      */
@@ -180,7 +180,8 @@ HSR_API int hsr_get_stats(hsr_stats* out);
 
 /* ---- timing of the last completed draw sequence (CUDA events on the library stream) --
  * batch_ms spans the upload of the view descriptors to the end of the raster kernel;
- * kernel_ms = {vertex, setup, scan, scatter, raster}, filled when profiling is on. */
+ * kernel_ms = {vertex, setup + post (clip / split), scan, scatter, raster}, filled when
+ * profiling is on. */
 typedef struct hsr_timing {
   float batch_ms;
   float kernel_ms[5];

@@ -48,7 +48,7 @@ def test_golden_fixture(gpu, name):
     assert_parity(gpu_render(gpu, frame), exp, name)
 
 
-@pytest.mark.parametrize("tile,warps", [(8, 4), (8, 8), (16, 4), (16, 8), (32, 4)])
+@pytest.mark.parametrize("tile,warps", [(8, 4), (8, 8), (16, 4), (16, 8)])
 def test_tile_configs_bit_identical(gpu, tile, warps):
     frame, exp = golden_io.load("plain_frame_ico4_512_blinn")
     old = gpu.get_tuning()
