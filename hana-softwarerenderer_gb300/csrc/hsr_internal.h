@@ -146,6 +146,7 @@ struct Scratch {
 int launch_vertex(const DView* views, const Chunk* chunks, int nchunks, cudaStream_t s);
 int launch_setup(const DView* views, const Chunk* chunks, int nchunks, int tile, Scratch sc, cudaStream_t s);
 int launch_post(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s);
+int launch_big(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s);
 int launch_scan(Scratch sc, cudaStream_t s);
 int launch_scatter(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s);
 int launch_raster(const DView* views, int tile, Scratch sc, int grid, int warps, cudaStream_t s);

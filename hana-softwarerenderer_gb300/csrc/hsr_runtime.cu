@@ -333,6 +333,8 @@ int Plan::enqueue(cudaStream_t s, int num_sms, const hsr_tuning& tu, cudaEvent_t
   if (kr) return cuda_fail((cudaError_t)kr, "setup kernel");
   kr = launch_post(dviews, tile, sc, num_sms * 2, s);
   if (kr) return cuda_fail((cudaError_t)kr, "post kernel");
+  kr = launch_big(dviews, tile, sc, num_sms * 2, s);
+  if (kr) return cuda_fail((cudaError_t)kr, "big-triangle kernel");
   if (ev && ev[3]) cudaEventRecord(ev[3], s);
   kr = launch_scan(sc, s);
   if (kr) return cuda_fail((cudaError_t)kr, "scan kernel");
@@ -349,7 +351,7 @@ int Plan::enqueue(cudaStream_t s, int num_sms, const hsr_tuning& tu, cudaEvent_t
 }
 
 int Plan::kernel_count() const {
-  return (vchunks.empty() ? 0 : 1) + (schunks.empty() ? 0 : 1) + 1 + (nscan > 0 ? 1 : 0) + 2;
+  return (vchunks.empty() ? 0 : 1) + (schunks.empty() ? 0 : 1) + 2 + (nscan > 0 ? 1 : 0) + 2;
 }
 
 // Grow the capacity an overflow reported; returns false if nothing overflowed.
@@ -756,6 +758,55 @@ int hsr_host_free(void* p) {
   if (!p) return HSR_OK;
   cudaError_t e = cudaFreeHost(p);
   return e == cudaSuccess ? HSR_OK : cuda_fail(e, "host_free");
+}
+
+// Autotuner: renders the batch with each candidate (tile 8/16, warps per CTA 4/8, CTAs per
+// SM 1..8), keeps the fastest median device time, and sizes the bin capacity from the
+// (triangle, tile) pairs it observed.  The batch's targets receive `reps` renders per
+// candidate.
+int hsr_autotune(const hsr_draw_desc* descs, int32_t n, int32_t reps, hsr_tuning* out) {
+  RT_OR_FAIL();
+  if (!descs || n <= 0 || reps <= 0) return fail(HSR_ERR_INVALID_ARG, "autotune: bad arguments");
+  const hsr_tuning saved = g_rt->tuning;
+  const bool saved_prof = g_rt->profiling;
+  g_rt->profiling = false;
+  hsr_tuning best = saved;
+  float best_ms = 1e30f;
+  double pairs_per_item = 0.0;
+  const int tiles[2] = {8, 16}, warps[2] = {4, 8}, ctas[4] = {1, 2, 4, 8};
+  for (int ti : tiles)
+    for (int wi : warps)
+      for (int ci : ctas) {
+        if (ci * wi > 32) continue;  // beyond one SM's warp slots for these kernels
+        hsr_tuning cand = saved;
+        cand.tile = ti;
+        cand.warps_per_cta = wi;
+        cand.ctas_per_sm = ci;
+        g_rt->tuning = cand;
+        std::vector<float> ms;
+        for (int r = 0; r < reps + 1; r++) {
+          int rc = g_rt->run_batch(descs, n);
+          if (rc != HSR_OK) {
+            g_rt->tuning = saved;
+            g_rt->profiling = saved_prof;
+            return rc;
+          }
+          if (r > 0) ms.push_back(g_rt->timing.batch_ms);  // first run warms up
+        }
+        std::sort(ms.begin(), ms.end());
+        const float med = ms[ms.size() / 2];
+        if (med < best_ms) {
+          best_ms = med;
+          best = cand;
+        }
+        const double items = (double)g_rt->timing.faces + (double)g_rt->timing.pixels / (double)(ti * ti);
+        if (items > 0) pairs_per_item = std::max(pairs_per_item, (double)g_rt->timing.bin_pairs / items);
+      }
+  best.bin_factor = (float)std::min(64.0, std::max(1.0, pairs_per_item * 1.25));
+  g_rt->tuning = best;
+  g_rt->profiling = saved_prof;
+  if (out) *out = best;
+  return HSR_OK;
 }
 
 int hsr_get_stats(hsr_stats* out) {

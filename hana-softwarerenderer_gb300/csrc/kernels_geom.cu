@@ -209,44 +209,6 @@ __device__ void append_small(bool valid, const RasterRec& r, const Payload& pl, 
   }
 }
 
-// Expand one triangle whose bounding box touches more than kMaxRecordTiles tiles into
-// sub-records over blocks of kSubTilesX x kSubTilesY tiles: same triangle constants and
-// seq, pixel range clipped to the block, one payload shared by all of them (stored at the
-// first sub-record's slot).  The union of the sub-ranges is the triangle's pixel range, so
-// every pixel is tested exactly once.  All 32 lanes call this with the same `b`;
-// `copy_payload(dst)` stores the payload (called by lane 0).
-template <class CopyPayload>
-__device__ void expand_big(const RasterRec& b, const DView& v, int T, const Scratch& sc, CopyPayload copy_payload) {
-  const int lane = threadIdx.x & 31;
-  int tx0, ty0, ntw, nt;
-  rec_tiles(b, T, tx0, ty0, ntw, nt);
-  const int nth = nt / ntw;
-  const int nbx = (ntw + kSubTilesX - 1) / kSubTilesX, nby = (nth + kSubTilesY - 1) / kSubTilesY;
-  const int nsub = nbx * nby;
-  uint32_t base = 0;
-  if (lane == 0) base = atomicAdd(&sc.ctl->rec_count, (uint32_t)nsub);
-  base = __shfl_sync(kFull, base, 0);
-  if ((uint64_t)base + (uint64_t)nsub > (uint64_t)sc.rec_cap) {
-    if (lane == 0) atomicOr(&sc.ctl->error, kErrRecOverflow);
-    return;
-  }
-  if (lane == 0) copy_payload(&sc.pay[base]);
-  const int x0 = (int)(b.xr & 0xffffu), x1 = (int)(b.xr >> 16);
-  const int y0 = (int)(b.yr & 0xffffu), y1 = (int)(b.yr >> 16);
-  for (int sidx = lane; sidx < nsub; sidx += 32) {
-    const int bx = sidx % nbx, by = sidx / nbx;
-    const int stx0 = tx0 + bx * kSubTilesX, stx1 = min(tx0 + ntw - 1, stx0 + kSubTilesX - 1);
-    const int sty0 = ty0 + by * kSubTilesY, sty1 = min(ty0 + nth - 1, sty0 + kSubTilesY - 1);
-    RasterRec w = b;
-    w.xr = (uint32_t)max(x0, stx0 * T) | ((uint32_t)min(x1, stx1 * T + T - 1) << 16);
-    w.yr = (uint32_t)max(y0, sty0 * T) | ((uint32_t)min(y1, sty1 * T + T - 1) << 16);
-    w.pad = base;
-    store_rec(&sc.recs[base + (uint32_t)sidx], w);
-    for (int ty = sty0; ty <= sty1; ty++)
-      for (int tx = stx0; tx <= stx1; tx++) atomicAdd(&sc.tile_count[v.tile_base + ty * v.tiles_x + tx], 1u);
-  }
-}
-
 enum { PW, PX, NX, PY, NY, PZ, NZ };
 
 // is_inside_plane (graphics.cpp:29-49) on clip coordinates c[0..3]
@@ -417,59 +379,92 @@ __device__ void clip_face(const DView& v, int view, int face, int T, const Scrat
   const bool big = valid && nt > kMaxRecordTiles;
   const int nf4 = payload_f4(v.shader);
   append_small(valid && !big, r, pl, nf4, v, T, sc);
-  unsigned bm = __ballot_sync(kFull, big);
-  while (bm) {
-    const int l = __ffs(bm) - 1;
-    bm &= bm - 1;
-    RasterRec b;
-    const uint32_t* srcw = reinterpret_cast<const uint32_t*>(&r);
-    uint32_t* dstw = reinterpret_cast<uint32_t*>(&b);
-#pragma unroll
-    for (int q = 0; q < 16; q++) dstw[q] = __shfl_sync(kFull, srcw[q], l);
-    // the payload lives in lane l's registers: hand it over through the lanes' shuffle
-    float pw[kPayloadFloats];
-#pragma unroll
-    for (int q = 0; q < kPayloadFloats; q++) pw[q] = __shfl_sync(kFull, pl.f[q], l);
-    expand_big(b, v, T, sc, [&](Payload* dstp) {
-      Payload tmp;
-#pragma unroll
-      for (int q = 0; q < kPayloadFloats; q++) tmp.f[q] = pw[q];
-      store_payload(dstp, tmp, nf4);
-    });
+  const uint32_t bslot = warp_append(big, &sc.ctl->big_count);
+  if (big) {
+    if (bslot < sc.big_cap) {
+      store_rec(&sc.bigq[bslot].rec, r);
+      store_payload(&sc.bigq[bslot].pay, pl, nf4);
+    } else {
+      atomicOr(&sc.ctl->error, kErrBigOverflow);
+    }
   }
   __syncwarp();
 }
 
 constexpr int kPostThreads = 256;
 
-// Drains the clip queue and the big-triangle queue of k_setup, one warp per item.
+// Drains the clip queue of k_setup, one warp per face.
 __global__ void __launch_bounds__(kPostThreads) k_post(const DView* __restrict__ views, int T, Scratch sc) {
   __shared__ float poly[kPostThreads / 32][2][16 * kPolyStride];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (sc.ctl->error & kErrCapacity) return;
   const uint32_t nclip = min(sc.ctl->clip_count, sc.clip_cap);
-  const uint32_t nbig = min(sc.ctl->big_count, sc.big_cap);
-  const uint32_t total = nclip + nbig;
   for (;;) {
     uint32_t item = 0;
     if (lane == 0) item = atomicAdd(&sc.ctl->post_next, 1u);
     item = __shfl_sync(kFull, item, 0);
-    if (item >= total) break;
-    if (item < nclip) {
-      const int2 vf = sc.clipq[item];
-      clip_face(views[vf.x], vf.x, vf.y, T, sc, poly[warp][0], poly[warp][1]);
-    } else {
-      const BigItem& bi = sc.bigq[item - nclip];
-      const RasterRec b = bi.rec;
-      const DView& v = views[b.view];
-      const int nf4 = payload_f4(v.shader);
-      expand_big(b, v, T, sc, [&](Payload* dstp) { store_payload(dstp, bi.pay, nf4); });
-    }
+    if (item >= nclip) break;
+    const int2 vf = sc.clipq[item];
+    clip_face(views[vf.x], vf.x, vf.y, T, sc, poly[warp][0], poly[warp][1]);
   }
 }
 
 int launch_post(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s) {
   k_post<<<grid, kPostThreads, 0, s>>>(views, tile, sc);
+  return (int)cudaGetLastError();
+}
+
+constexpr int kBigThreads = 512;
+
+// Expands each queued huge triangle with a whole CTA: its tile rectangle splits into
+// sub-records over blocks of kSubTilesX x kSubTilesY tiles (same triangle constants and
+// seq, pixel range clipped to the block, one shared payload at the first sub-record's
+// slot), and every tile of the rectangle is counted once.  The sub-ranges partition the
+// triangle's pixel range, so each pixel is still tested exactly once.
+__global__ void __launch_bounds__(kBigThreads) k_big(const DView* __restrict__ views, int T, Scratch sc) {
+  __shared__ uint32_t s_base;
+  if (sc.ctl->error & kErrCapacity) return;
+  const uint32_t nbig = min(sc.ctl->big_count, sc.big_cap);
+  for (uint32_t item = blockIdx.x; item < nbig; item += gridDim.x) {
+    const BigItem& bi = sc.bigq[item];
+    const RasterRec b = bi.rec;
+    const DView& v = views[b.view];
+    int tx0, ty0, ntw, nt;
+    rec_tiles(b, T, tx0, ty0, ntw, nt);
+    const int nth = nt / ntw;
+    const int nbx = (ntw + kSubTilesX - 1) / kSubTilesX, nby = (nth + kSubTilesY - 1) / kSubTilesY;
+    const int nsub = nbx * nby;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const uint32_t base = atomicAdd(&sc.ctl->rec_count, (uint32_t)nsub);
+      s_base = base;
+      if ((uint64_t)base + (uint64_t)nsub > (uint64_t)sc.rec_cap) atomicOr(&sc.ctl->error, kErrRecOverflow);
+    }
+    __syncthreads();
+    const uint32_t base = s_base;
+    if ((uint64_t)base + (uint64_t)nsub > (uint64_t)sc.rec_cap) continue;
+    const int nf4 = payload_f4(v.shader);
+    if ((int)threadIdx.x < nf4)
+      reinterpret_cast<float4*>(&sc.pay[base])[threadIdx.x] = reinterpret_cast<const float4*>(&bi.pay)[threadIdx.x];
+    const int x0 = (int)(b.xr & 0xffffu), x1 = (int)(b.xr >> 16);
+    const int y0 = (int)(b.yr & 0xffffu), y1 = (int)(b.yr >> 16);
+    for (int sidx = threadIdx.x; sidx < nsub; sidx += kBigThreads) {
+      const int bx = sidx % nbx, by = sidx / nbx;
+      const int stx0 = tx0 + bx * kSubTilesX, stx1 = min(tx0 + ntw - 1, stx0 + kSubTilesX - 1);
+      const int sty0 = ty0 + by * kSubTilesY, sty1 = min(ty0 + nth - 1, sty0 + kSubTilesY - 1);
+      RasterRec w = b;
+      w.xr = (uint32_t)max(x0, stx0 * T) | ((uint32_t)min(x1, stx1 * T + T - 1) << 16);
+      w.yr = (uint32_t)max(y0, sty0 * T) | ((uint32_t)min(y1, sty1 * T + T - 1) << 16);
+      w.pad = base;
+      store_rec(&sc.recs[base + (uint32_t)sidx], w);
+    }
+    for (int k = threadIdx.x; k < nt; k += kBigThreads)
+      atomicAdd(&sc.tile_count[v.tile_base + (ty0 + k / ntw) * v.tiles_x + tx0 + k % ntw], 1u);
+  }
+}
+
+int launch_big(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s) {
+  k_big<<<grid, kBigThreads, 0, s>>>(views, tile, sc);
   return (int)cudaGetLastError();
 }
 

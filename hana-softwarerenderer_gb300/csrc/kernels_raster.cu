@@ -145,11 +145,17 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
   if (sc.ctl->error & kErrCapacity) return;
   const uint32_t nrec = min(sc.ctl->rec_count, sc.rec_cap);
 
+  uint32_t t = 0;
+  if (lane == 0) t = atomicAdd(&sc.ctl->tile_next, 1u);
+  t = __shfl_sync(kFull, t, 0);
   for (;;) {
-    uint32_t t = 0;
-    if (lane == 0) t = atomicAdd(&sc.ctl->tile_next, 1u);
-    t = __shfl_sync(kFull, t, 0);
     if ((int)t >= sc.ntiles) break;
+    // grab the next tile now, use it after this one: the atomic's latency overlaps the work
+    // (dependencies only point to lower tile indices, so holding a later tile never blocks)
+    uint32_t t_next = 0;
+    if (lane == 0) t_next = atomicAdd(&sc.ctl->tile_next, 1u);
+    const uint32_t n = sc.tile_count[t];
+    const uint32_t off = sc.tile_off[t];
     const int vi = find_view(views, sc.nviews, (int)t);
     const DView& v = views[vi];
     if (lane == 0) {
@@ -161,7 +167,6 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
     const int tx = lt % v.tiles_x, ty = lt / v.tiles_x;
     const int ox = tx * T, oy = ty * T;
     const bool clear = (v.flags & HSR_DRAW_CLEAR) != 0u;
-    const uint32_t n = sc.tile_count[t];
 
     if (n == 0) {
       if (clear) {
@@ -187,7 +192,6 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
         skey[warp][p] = buffer_key(d);
         swin[warp][p] = 0xffffffffu;
       }
-      const uint32_t off = sc.tile_off[t];
       for (uint32_t b = 0; b < n; b += 32) {
         const uint32_t cnt = min(32u, n - b);
         uint32_t c = 0;
@@ -322,7 +326,7 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
       __syncwarp();
       if (lane == 0) atomicAdd(&sc.view_done[vi], 1u);
     }
-    __syncwarp();
+    t = __shfl_sync(kFull, t_next, 0);
   }
 }
 

@@ -100,6 +100,8 @@ def lib():
         "hsr_set_tuning": ([ctypes.POINTER(Tuning)], ctypes.c_int),
         "hsr_get_stats": ([ctypes.POINTER(Stats)], ctypes.c_int),
         "hsr_set_profiling": ([ctypes.c_int], ctypes.c_int),
+        "hsr_autotune": ([ctypes.POINTER(DrawDesc), ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(Tuning)],
+                         ctypes.c_int),
         "hsr_last_timing": ([ctypes.POINTER(Timing)], ctypes.c_int),
         "hsr_host_alloc": ([ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
         "hsr_host_free": ([ctypes.c_void_p], ctypes.c_int),
@@ -146,6 +148,14 @@ def set_tuning(tile=None, ctas_per_sm=None, warps_per_cta=None, bin_factor=None)
     if bin_factor is not None:
         t.bin_factor = bin_factor
     check(lib().hsr_set_tuning(ctypes.byref(t)))
+
+
+def autotune(descs, reps: int = 3) -> dict:
+    """Time the batch under each tuning candidate and keep the fastest (hsr_autotune)."""
+    arr = (DrawDesc * len(descs))(*descs)
+    t = Tuning()
+    check(lib().hsr_autotune(arr, len(descs), reps, ctypes.byref(t)))
+    return {k: getattr(t, k) for k, _ in Tuning._fields_}
 
 
 def stats() -> dict:

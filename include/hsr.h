@@ -166,6 +166,10 @@ typedef struct hsr_tuning {
 } hsr_tuning;
 HSR_API int hsr_get_tuning(hsr_tuning* out);
 HSR_API int hsr_set_tuning(const hsr_tuning* in);
+/* Pick tile size, warps per CTA and CTAs per SM by timing the given batch (each candidate
+ * renders it `reps` times into its targets), set them, size the bin capacity from the
+ * observed (triangle, tile) pairs, and return the choice in `out` (may be NULL). */
+HSR_API int hsr_autotune(const hsr_draw_desc* descs, int32_t n, int32_t reps, hsr_tuning* out);
 
 /* ---- statistics of the last completed draw sequence (for tests and benchmarks) ------- */
 typedef struct hsr_stats {

@@ -219,3 +219,22 @@ def test_empty_mesh_only_clears(gpu):
         tgt.release()
     assert (got["color"] == np.array([1, 2, 3, 4], np.uint8)).all()
     assert (got["depth"] == np.float32(0.5)).all() and (got["prim"] == 0).all()
+
+
+def test_autotune_picks_a_valid_config_and_stays_exact(gpu):
+    import hsr
+
+    frame, exp = golden_io.load("displaced4_normalmap_shadow")
+    old = gpu.get_tuning()
+    g = hframe.GpuFrame(frame)
+    try:
+        best = hsr.autotune(g.descs, reps=2)
+        assert best["tile"] in (8, 16) and best["warps_per_cta"] in (4, 8) and 1 <= best["ctas_per_sm"] <= 8
+        assert best["bin_factor"] >= 1.0
+        g.render()
+        got = g.download()
+    finally:
+        g.release()
+        gpu.set_tuning(tile=old.tile, warps_per_cta=old.warps_per_cta, ctas_per_sm=old.ctas_per_sm,
+                       bin_factor=old.bin_factor)
+    assert_parity(got, exp, f"autotuned {best}")
