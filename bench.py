@@ -179,7 +179,7 @@ def run_ours(args, world, rank, local):
 
     tuned = None
     if args.tile:
-        hsr.set_tuning(tile=args.tile)
+        hsr.set_tuning(tile=args.tile, warps_per_cta=4 if args.tile == 16 else 8)
     elif not args.no_autotune:
         tuned = hsr.autotune(g.descs, reps=3)  # outside the timed region
     hsr.set_profiling(True)

@@ -51,7 +51,7 @@ __device__ __forceinline__ F3 cross3(F3 a, F3 b) {  // vector.h:97-99
 }
 __device__ __forceinline__ F3 normalize3(F3 v) {  // vector.h:41-42
   float n = __fsqrt_rn(fa(fa(fm(v.x, v.x), fm(v.y, v.y)), fm(v.z, v.z)));
-  float f = fd(1.f, n);
+  float f = __frcp_rn(n);  // 1.f / n, correctly rounded
   return {fm(v.x, f), fm(v.y, f), fm(v.z, f)};
 }
 // Matrix4x4 * Vector4f row by row (matrix.h:112-116); m row-major.
@@ -74,6 +74,40 @@ __device__ __forceinline__ Col c_mulf(Col a, float t) {
 __device__ __forceinline__ Col c_mulc(Col a, Col b) { return {fm(a.r, b.r), fm(a.g, b.g), fm(a.b, b.b), fm(a.a, b.a)}; }
 __device__ __forceinline__ Col c_of(const float* p) { return {p[0], p[1], p[2], p[3]}; }
 
+// ---- division --------------------------------------------------------------------------
+// a / b rounded to nearest, given y = RN(1/b) (__frcp_rn), by Markstein's theorem
+// (P. Markstein, IBM J. Res. Dev. 34(1), 1990; also Muller et al., Handbook of
+// Floating-Point Arithmetic, the "Markstein iteration"): if y is the correctly rounded
+// reciprocal and q is within one ulp of a/b, the remainder r = a - b*q is exact in an FMA
+// and RN(q + r*y) is the correctly rounded quotient.  One refinement step brings
+// q0 = RN(a*y) (within two ulps) within one ulp, the second step rounds correctly.  Valid
+// while no intermediate overflows or underflows, which the raster guarantees by routing
+// records outside its coordinate range to the literal division (kRecExact).  A device
+// self-test compares it with __fdiv_rn (hsr_selftest).
+__device__ __forceinline__ float div_m(float a, float b, float y) {
+  float q = __fmul_rn(a, y);
+  float r = __fmaf_rn(-b, q, a);
+  q = __fmaf_rn(r, y, q);
+  r = __fmaf_rn(-b, q, a);
+  return __fmaf_rn(r, y, q);
+}
+
+// ---- byte -> float tables --------------------------------------------------------------
+// Colour channels and normal-map components are bytes; their float values are the IEEE
+// results b/255.f (color.cpp:5, renderbuffer.cpp:46) and (b/255.f)*2.f - 1.f
+// (IShader.h:97), computed once per CTA into shared memory with the same operations.
+struct ByteTables {
+  const float* u8f;  // b / 255.f
+  const float* u8n;  // (b / 255.f) * 2.f - 1.f
+};
+__device__ __forceinline__ void build_byte_tables(float* u8f, float* u8n) {
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+    const float f = fd((float)i, 255.f);
+    u8f[i] = f;
+    u8n[i] = fs(fm(f, 2.f), 1.f);
+  }
+}
+
 // ---- textures: TGAImage::get (tgaimage.cpp:248-253) on BGRA words ------------------------
 // Texels are stored as 32-bit words b | g<<8 | r<<16 | a<<24 with missing bytes zero,
 // which is what TGAColor(p, bytespp) holds for bytespp 1, 3 and 4.
@@ -82,18 +116,17 @@ __device__ __forceinline__ uint32_t tga_get(const uint32_t* tex, int32_t w, int3
   return __ldg(tex + (size_t)y * (size_t)w + (size_t)x);
 }
 // IShader::tex_diffuse (IShader.h:85-89), Color(TGAColor) (color.cpp:5)
-__device__ __forceinline__ Col tex_diffuse(const DView& v, float u, float t) {
+__device__ __forceinline__ Col tex_diffuse(const DView& v, float u, float t, const ByteTables& bt) {
   uint32_t c = tga_get(v.diffuse, v.dw, v.dh, cvt_i32(fm(u, (float)v.dw)), cvt_i32(fm(t, (float)v.dh)));
-  return {fd((float)((c >> 16) & 255u), 255.f), fd((float)((c >> 8) & 255u), 255.f),
-          fd((float)(c & 255u), 255.f), fd((float)(c >> 24), 255.f)};
+  return {bt.u8f[(c >> 16) & 255u], bt.u8f[(c >> 8) & 255u], bt.u8f[c & 255u], bt.u8f[c >> 24]};
 }
 // IShader::tex_normal (IShader.h:91-99)
-__device__ __forceinline__ F3 tex_normal(const DView& v, float u, float t) {
+__device__ __forceinline__ F3 tex_normal(const DView& v, float u, float t, const ByteTables& bt) {
   uint32_t c = tga_get(v.normal, v.nw, v.nh, cvt_i32(fm(u, (float)v.nw)), cvt_i32(fm(t, (float)v.nh)));
   F3 r;
-  r.z = fs(fm(fd((float)(c & 255u), 255.f), 2.f), 1.f);
-  r.y = fs(fm(fd((float)((c >> 8) & 255u), 255.f), 2.f), 1.f);
-  r.x = fs(fm(fd((float)((c >> 16) & 255u), 255.f), 2.f), 1.f);
+  r.z = bt.u8n[c & 255u];
+  r.y = bt.u8n[(c >> 8) & 255u];
+  r.x = bt.u8n[(c >> 16) & 255u];
   return r;
 }
 
@@ -102,9 +135,9 @@ __device__ __forceinline__ F3 viewport(int32_t w, int32_t h, F3 ndc) {
   return {fm(fm(fa(ndc.x, 1.f), 0.5f), (float)w), fm(fm(fa(ndc.y, 1.f), 0.5f), (float)h), fm(fa(ndc.z, 1.f), 0.5f)};
 }
 
-// IShader::is_in_shadow (IShader.h:107-129).  The shadow map's colour plane may have been
-// written earlier in the same launch by other warps: read it past L1 (ld.global.cg).
-__device__ __forceinline__ int is_in_shadow(const DView& v, float4 dp, float n_dot_l) {
+// IShader::is_in_shadow (IShader.h:107-129).  The shadow map's colour plane was written by
+// an earlier view of the batch: read it past L1 (ld.global.cg).
+__device__ __forceinline__ int is_in_shadow(const DView& v, float4 dp, float n_dot_l, const ByteTables& bt) {
   if (v.u.enable_shadow && v.sm_color) {
     float widht = (float)v.smW, height = (float)v.smH;
     F3 ndc = {fd(dp.x, dp.w), fd(dp.y, dp.w), fd(dp.z, dp.w)};
@@ -116,47 +149,64 @@ __device__ __forceinline__ int is_in_shadow(const DView& v, float4 dp, float n_d
     if (pos.x != pos.x || pos.y != pos.y) return 1;  // NaN: undefined in the reference; lit
     int32_t x = cvt_i32(pos.x), y = cvt_i32(pos.y);
     uint32_t word = __ldcg(v.sm_color + (size_t)y * (size_t)v.smW + (size_t)x);
-    float closest_depth = fd((float)(word & 255u), 255.f);
+    float closest_depth = bt.u8f[word & 255u];
     return current_depth < closest_depth;
   }
   return 1;
 }
 
 // ---- fragment shaders (IShader.cpp) ---------------------------------------------------------
-// Interpolated varyings the fragment stage reads (shader_struct_v2f layout).
-struct Frag {
-  float clip_z;           // [2]
-  F3 wpos;                // [4..6]
-  F3 wnrm;                // [7..9]
-  float u, t;             // [10..11]
-  float intensity;        // [12]
-};
+// Perspective-correct interpolation (graphics.cpp:205-220) of the varyings a shader reads,
+// from the record's payload (Payload layout in hsr_internal.h) and the pixel's barycentric
+// weights, then the fragment shader.  Specialised per shader at compile time so each one
+// interpolates only what it reads (every float interpolates independently, so skipping
+// the others changes no bit).
+__device__ __forceinline__ float interp(float s0, float s1, float s2, float w0, float w1, float w2, float nrm) {
+  return fm(fa(fa(fm(s0, w0), fm(s1, w1)), fm(s2, w2)), nrm);
+}
+
+// Payload float4s a shader reads (layout in hsr_internal.h).
+template <int S> __device__ __forceinline__ constexpr int payload_f4_of() {
+  return S == HSR_SHADER_FLAT ? 0
+       : (S == HSR_SHADER_SHADOW || S == HSR_SHADER_GROUND || S == HSR_SHADER_TOON) ? 2
+       : S == HSR_SHADER_TEXTURE ? 3
+       : S == HSR_SHADER_TEXTURE_WITH_LIGHT ? 6 : 8;
+}
 
 // Blinn-Phong tail shared by BlinnShader and NormalMapShader (IShader.cpp:94-109, :146-162).
-__device__ __forceinline__ Col lit(const DView& v, F3 N, const Frag& f) {
-  const hsr_shader_data& u = v.u;
-  F3 L = {u.light_dir[0], u.light_dir[1], u.light_dir[2]};
-  F3 vp = {u.view_pos[0], u.view_pos[1], u.view_pos[2]};
-  Col albedo = c_mulc(tex_diffuse(v, f.u, f.t), c_of(u.material_color));
-  Col ambient = c_mulc(c_of(u.ambient), albedo);
+__device__ __forceinline__ Col lit(const DView& v, F3 N, F3 wpos, float u, float t, const ByteTables& bt) {
+  const hsr_shader_data& un = v.u;
+  F3 L = {un.light_dir[0], un.light_dir[1], un.light_dir[2]};
+  F3 vp = {un.view_pos[0], un.view_pos[1], un.view_pos[2]};
+  Col albedo = c_mulc(tex_diffuse(v, u, t, bt), c_of(un.material_color));
+  Col ambient = c_mulc(c_of(un.ambient), albedo);
   float n_dot_l = saturate(dot3(N, L));
-  Col diffuse = c_mulf(c_mulc(c_of(u.light_color), albedo), n_dot_l);
-  F3 view_dir = normalize3(sub3(vp, f.wpos));
+  Col diffuse = c_mulf(c_mulc(c_of(un.light_color), albedo), n_dot_l);
+  F3 view_dir = normalize3(sub3(vp, wpos));
   F3 half_dir = normalize3(add3(view_dir, L));
-  Col spec = c_mulf(c_mulc(c_of(u.light_color), c_of(u.material_specular)),
-                    powf(saturate(dot3(N, half_dir)), u.gloss));
-  float4 depth_pos = mat_vec(u.light_vp_matrix, f.wpos.x, f.wpos.y, f.wpos.z, 1.f);
-  int shadow = is_in_shadow(v, depth_pos, n_dot_l);
+  Col spec = c_mulf(c_mulc(c_of(un.light_color), c_of(un.material_specular)),
+                    powf(saturate(dot3(N, half_dir)), un.gloss));
+  float4 depth_pos = mat_vec(un.light_vp_matrix, wpos.x, wpos.y, wpos.z, 1.f);
+  int shadow = is_in_shadow(v, depth_pos, n_dot_l, bt);
   return c_add(ambient, c_mulf(c_add(diffuse, spec), (float)shadow));
 }
 
-__device__ __forceinline__ Col fragment(const DView& v, const Frag& f, uint32_t prim) {
+template <int S>
+__device__ __forceinline__ Col fragment_s(const DView& v, const float* P, float b0, float b1, float b2, uint32_t prim,
+                                          const ByteTables& bt) {
   const Col white = {1.f, 1.f, 1.f, 255.f};
-  switch (v.shader) {
-    case HSR_SHADER_GROUND:  // IShader.cpp:12-15
-      return c_mulf(white, f.intensity);
-    case HSR_SHADER_TOON: {  // IShader.cpp:30-39 (double compares, as written)
-      float intensity = f.intensity;
+  if constexpr (S == HSR_SHADER_FLAT) {  // test shader: bytes of the prim id
+    return {fd(fa((float)(prim & 255u), 0.5f), 255.f), fd(fa((float)((prim >> 8) & 255u), 0.5f), 255.f),
+            fd(fa((float)((prim >> 16) & 255u), 0.5f), 255.f), 255.f};
+  } else {
+    const float w0 = fm(P[0], b0), w1 = fm(P[1], b1), w2 = fm(P[2], b2);
+    const float nrm = __frcp_rn(fa(fa(w0, w1), w2));
+    if constexpr (S == HSR_SHADER_SHADOW) {  // IShader.cpp:176-180
+      return c_mulf(white, interp(P[3], P[4], P[5], w0, w1, w2, nrm));
+    } else if constexpr (S == HSR_SHADER_GROUND) {  // IShader.cpp:12-15
+      return c_mulf(white, interp(P[3], P[4], P[5], w0, w1, w2, nrm));
+    } else if constexpr (S == HSR_SHADER_TOON) {  // IShader.cpp:30-39 (double compares, as written)
+      float intensity = interp(P[3], P[4], P[5], w0, w1, w2, nrm);
       if ((double)intensity > .85) intensity = 1.f;
       else if ((double)intensity > .60) intensity = (float).80;
       else if ((double)intensity > .45) intensity = (float).60;
@@ -164,35 +214,39 @@ __device__ __forceinline__ Col fragment(const DView& v, const Frag& f, uint32_t 
       else if ((double)intensity > .15) intensity = (float).30;
       Col base = {1.f, fd(155.f, 255.f), 0.f, 255.f};
       return c_mulf(base, intensity);
-    }
-    case HSR_SHADER_TEXTURE:  // IShader.cpp:54-57
-      return tex_diffuse(v, f.u, f.t);
-    case HSR_SHADER_TEXTURE_WITH_LIGHT: {  // IShader.cpp:73-77
-      F3 L = {v.u.light_dir[0], v.u.light_dir[1], v.u.light_dir[2]};
-      return c_mulf(tex_diffuse(v, f.u, f.t), saturate(dot3(f.wnrm, L)));
-    }
-    case HSR_SHADER_BLINN:  // IShader.cpp:94-109
-      return lit(v, normalize3(f.wnrm), f);
-    case HSR_SHADER_NORMALMAP: {  // IShader.cpp:126-162
-      F3 n = f.wnrm;
-      float x = n.x, y = n.y, z = n.z;
-      float sq = __fsqrt_rn(fa(fm(x, x), fm(z, z)));
-      F3 t = {fd(fm(x, y), sq), sq, fd(fm(z, y), sq)};
-      F3 b = cross3(n, t);
-      F3 r0 = {t.x, b.x, n.x}, r1 = {t.y, b.y, n.y}, r2 = {t.z, b.z, n.z};
-      F3 bump = tex_normal(v, f.u, f.t);
-      bump.x = fm(bump.x, v.u.bump_scale);
-      bump.y = fm(bump.y, v.u.bump_scale);
-      float bb = fa(fa(0.f, fm(bump.y, bump.y)), fm(bump.x, bump.x));
-      bump.z = __double2float_rn(__dsqrt_rn(__dsub_rn(1.0, (double)saturate(bb))));
-      F3 tn = {dot3(r0, bump), dot3(r1, bump), dot3(r2, bump)};
-      return lit(v, normalize3(tn), f);
-    }
-    case HSR_SHADER_SHADOW:  // IShader.cpp:176-180
-      return c_mulf(white, f.clip_z);
-    default: {  // FLAT (test shader): bytes of the prim id
-      return {fd(fa((float)(prim & 255u), 0.5f), 255.f), fd(fa((float)((prim >> 8) & 255u), 0.5f), 255.f),
-              fd(fa((float)((prim >> 16) & 255u), 0.5f), 255.f), 255.f};
+    } else {
+      const float u = interp(P[6], P[8], P[10], w0, w1, w2, nrm);
+      const float t = interp(P[7], P[9], P[11], w0, w1, w2, nrm);
+      if constexpr (S == HSR_SHADER_TEXTURE) {  // IShader.cpp:54-57
+        return tex_diffuse(v, u, t, bt);
+      } else {
+        const F3 wn = {interp(P[12], P[15], P[18], w0, w1, w2, nrm), interp(P[13], P[16], P[19], w0, w1, w2, nrm),
+                       interp(P[14], P[17], P[20], w0, w1, w2, nrm)};
+        if constexpr (S == HSR_SHADER_TEXTURE_WITH_LIGHT) {  // IShader.cpp:73-77
+          F3 L = {v.u.light_dir[0], v.u.light_dir[1], v.u.light_dir[2]};
+          return c_mulf(tex_diffuse(v, u, t, bt), saturate(dot3(wn, L)));
+        } else {
+          const F3 wp = {interp(P[21], P[24], P[27], w0, w1, w2, nrm), interp(P[22], P[25], P[28], w0, w1, w2, nrm),
+                         interp(P[23], P[26], P[29], w0, w1, w2, nrm)};
+          if constexpr (S == HSR_SHADER_BLINN) {  // IShader.cpp:94-109
+            return lit(v, normalize3(wn), wp, u, t, bt);
+          } else {  // NormalMapShader, IShader.cpp:126-162
+            F3 n = wn;
+            float x = n.x, y = n.y, z = n.z;
+            float sq = __fsqrt_rn(fa(fm(x, x), fm(z, z)));
+            F3 tg = {fd(fm(x, y), sq), sq, fd(fm(z, y), sq)};
+            F3 b = cross3(n, tg);
+            F3 r0 = {tg.x, b.x, n.x}, r1 = {tg.y, b.y, n.y}, r2 = {tg.z, b.z, n.z};
+            F3 bump = tex_normal(v, u, t, bt);
+            bump.x = fm(bump.x, v.u.bump_scale);
+            bump.y = fm(bump.y, v.u.bump_scale);
+            float bb = fa(fa(0.f, fm(bump.y, bump.y)), fm(bump.x, bump.x));
+            bump.z = __double2float_rn(__dsqrt_rn(__dsub_rn(1.0, (double)saturate(bb))));
+            F3 tn = {dot3(r0, bump), dot3(r1, bump), dot3(r2, bump)};
+            return lit(v, normalize3(tn), wp, u, t, bt);
+          }
+        }
+      }
     }
   }
 }
@@ -203,17 +257,6 @@ __device__ __forceinline__ uint32_t pack_rgb(Col c, uint32_t alpha_word) {
   uint32_t g = (uint32_t)cvt_i32(fm(c.g, 255.f)) & 255u;
   uint32_t b = (uint32_t)cvt_i32(fm(c.b, 255.f)) & 255u;
   return r | (g << 8) | (b << 16) | (alpha_word & 0xFF000000u);
-}
-
-// Varyings each shader reads: which corner streams the shading stage interpolates.
-__device__ __forceinline__ bool needs_wpos(int s) { return s == HSR_SHADER_BLINN || s == HSR_SHADER_NORMALMAP; }
-__device__ __forceinline__ bool needs_wnrm(int s) {
-  return s == HSR_SHADER_GROUND || s == HSR_SHADER_TOON || s == HSR_SHADER_TEXTURE_WITH_LIGHT ||
-         s == HSR_SHADER_BLINN || s == HSR_SHADER_NORMALMAP;
-}
-__device__ __forceinline__ bool needs_uv(int s) {
-  return s == HSR_SHADER_TEXTURE || s == HSR_SHADER_TEXTURE_WITH_LIGHT || s == HSR_SHADER_BLINN ||
-         s == HSR_SHADER_NORMALMAP;
 }
 
 }  // namespace hsr

@@ -724,6 +724,7 @@ int hsr_set_tuning(const hsr_tuning* in) {
   if (!in) return fail(HSR_ERR_INVALID_ARG, "set_tuning: null");
   if (in->tile != 8 && in->tile != 16) return fail(HSR_ERR_INVALID_ARG, "set_tuning: tile must be 8 or 16");
   if (in->warps_per_cta != 4 && in->warps_per_cta != 8) return fail(HSR_ERR_INVALID_ARG, "set_tuning: warps_per_cta must be 4 or 8");
+  if (in->tile == 16 && in->warps_per_cta != 4) return fail(HSR_ERR_INVALID_ARG, "set_tuning: tile 16 runs 4 warps per CTA");
   if (in->ctas_per_sm < 1 || in->ctas_per_sm > 16) return fail(HSR_ERR_INVALID_ARG, "set_tuning: ctas_per_sm in [1,16]");
   if (!(in->bin_factor >= 0.5f && in->bin_factor <= 64.f)) return fail(HSR_ERR_INVALID_ARG, "set_tuning: bin_factor in [0.5,64]");
   g_rt->tuning = *in;
@@ -778,6 +779,7 @@ int hsr_autotune(const hsr_draw_desc* descs, int32_t n, int32_t reps, hsr_tuning
     for (int wi : warps)
       for (int ci : ctas) {
         if (ci * wi > 32) continue;  // beyond one SM's warp slots for these kernels
+        if (ti == 16 && wi != 4) continue;  // shared-memory budget of the 16x16 tile
         hsr_tuning cand = saved;
         cand.tile = ti;
         cand.warps_per_cta = wi;
@@ -806,6 +808,23 @@ int hsr_autotune(const hsr_draw_desc* descs, int32_t n, int32_t reps, hsr_tuning
   g_rt->tuning = best;
   g_rt->profiling = saved_prof;
   if (out) *out = best;
+  return HSR_OK;
+}
+
+int hsr_selftest_division(uint64_t n, uint64_t seed, uint64_t* mismatches) {
+  RT_OR_FAIL();
+  if (!mismatches) return fail(HSR_ERR_INVALID_ARG, "selftest_division: null");
+  unsigned long long* d = nullptr;
+  int rc = g_rt->arena.reserve(sizeof(unsigned long long));
+  if (rc != HSR_OK) return rc;
+  d = reinterpret_cast<unsigned long long*>(g_rt->arena.base);
+  cudaError_t e = cudaMemsetAsync(d, 0, sizeof(*d), g_rt->stream);
+  if (e == cudaSuccess) e = (cudaError_t)launch_selftest_div(n, seed, d, g_rt->stream);
+  unsigned long long h = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, g_rt->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(g_rt->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "selftest_division");
+  *mismatches = h;
   return HSR_OK;
 }
 

@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(256) k_scatter(const DView* __restrict__ views
     if (ok) {
       const RasterRec& r = sc.recs[i];
       const uint32_t xr = r.xr, yr = r.yr;
-      const DView& v = views[r.view];
+      const DView& v = views[r.view & kRecViewMask];
       tbase = v.tile_base;
       tiles_x = v.tiles_x;
       tx0 = (int)(xr & 0xffffu) / T;

@@ -114,12 +114,13 @@ __device__ __forceinline__ bool build_rec(const DView& v, float4 c0, float4 c1, 
   r.ax = s0.x; r.ay = s0.y; r.e1x = e1x; r.e1y = e1y;
   r.e2x = e2x; r.e2y = e2y; r.uz = uz; r.d0 = s0.z;
   r.d1 = s1.z; r.d2 = s2.z;
-  r.seq = seq; r.view = view;
+  r.seq = seq;
   r.xr = (uint32_t)x0 | ((uint32_t)x1 << 16);
   r.yr = (uint32_t)y0 | ((uint32_t)y1 << 16);
   const bool ok = coord_ok(s0.x) && coord_ok(s0.y) && coord_ok(s1.x) && coord_ok(s1.y) &&
                   coord_ok(s2.x) && coord_ok(s2.y) && fabsf(uz) <= 0x1p30f;
-  r.flags = ok ? 0u : kRecExact;
+  r.view = view | ((ok ? 0u : kRecExact) << kRecFlagShift);
+  r.ruz = __frcp_rn(uz);
   r.pad = 0u;
   return true;
 }
@@ -428,7 +429,7 @@ __global__ void __launch_bounds__(kBigThreads) k_big(const DView* __restrict__ v
   for (uint32_t item = blockIdx.x; item < nbig; item += gridDim.x) {
     const BigItem& bi = sc.bigq[item];
     const RasterRec b = bi.rec;
-    const DView& v = views[b.view];
+    const DView& v = views[b.view & kRecViewMask];
     int tx0, ty0, ntw, nt;
     rec_tiles(b, T, tx0, ty0, ntw, nt);
     const int nth = nt / ntw;

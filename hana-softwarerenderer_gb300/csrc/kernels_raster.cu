@@ -8,9 +8,9 @@
 // (interpolate_depth starts from +0), so the order-independent rule
 //     min over (depth, later-submitted)
 // with the buffer's depth as the weakest entry reproduces the loop exactly, whatever
-// order the tile lists hold.  All shaders return
-// `discard = false` and have no side effects (IShader.cpp:14,38,56,76,108,161,179), so
-// shading only the winner equals shading every passing fragment in order.
+// order the tile lists hold.  All shaders return `discard = false` and have no side
+// effects (IShader.cpp:14,38,56,76,108,161,179), so shading only the winner equals
+// shading every passing fragment in order.
 //
 // Coverage.  barycentric() (graphics.cpp:222-233) divides by u.z three times per pixel.
 // With u = (ux, uy, uz) and s = ux + uy (all rounded exactly as there),
@@ -19,7 +19,7 @@
 // so the test needs no division.  The equivalence holds when nonzero |ux|, |uy| cannot
 // underflow after the division; setup marks records outside that range (kRecExact) and
 // those evaluate the reference's divisions literally.  Covered pixels then compute the
-// three quotients exactly for the depth.
+// three quotients exactly for the depth (div_m with the record's RN(1/uz)).
 #include <float.h>
 
 #include "hsr_device.cuh"
@@ -28,54 +28,7 @@ namespace hsr {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr long kWaitLimit = 1L << 23;  // ~1-2 s of polling before a dependency wait gives up
-
-// interpolate_varyings (graphics.cpp:205-220) for one float
-__device__ __forceinline__ float interp(float s0, float s1, float s2, float w0, float w1, float w2, float nrm) {
-  return fm(fa(fa(fm(s0, w0), fm(s1, w1)), fm(s2, w2)), nrm);
-}
-
-// Barycentric weights at integer pixel P (graphics.cpp:222-233) for a covered pixel.
-__device__ __forceinline__ void bary(const RasterRec& r, float px, float py, float& b0, float& b1, float& b2) {
-  const float dx = fs(r.ax, px), dy = fs(r.ay, py);
-  const float ux = fs(fm(r.e1x, dy), fm(dx, r.e1y));
-  const float uy = fs(fm(dx, r.e2y), fm(r.e2x, dy));
-  b0 = fs(1.f, fd(fa(ux, uy), r.uz));
-  b1 = fd(uy, r.uz);
-  b2 = fd(ux, r.uz);
-}
-
-// Shade one pixel from its winning record and that record's payload (Payload layout in
-// hsr_internal.h): perspective-correct varyings, then the fragment shader.
-__device__ __forceinline__ uint32_t shade_pixel(const DView& v, const RasterRec& r, const float* P, int x, int y,
-                                                uint32_t alpha_word) {
-  const uint32_t prim = v.prim_base + (r.seq >> 4) + 1u;
-  if (v.shader == HSR_SHADER_FLAT) return pack_rgb(fragment(v, Frag{}, prim), alpha_word);
-  float b0, b1, b2;
-  bary(r, (float)x, (float)y, b0, b1, b2);
-  const float w0 = fm(P[0], b0), w1 = fm(P[1], b1), w2 = fm(P[2], b2);
-  const float nrm = fd(1.f, fa(fa(w0, w1), w2));
-  Frag f;
-  const float sc = interp(P[3], P[4], P[5], w0, w1, w2, nrm);
-  f.clip_z = sc;
-  f.intensity = sc;
-  f.u = interp(P[6], P[8], P[10], w0, w1, w2, nrm);
-  f.t = interp(P[7], P[9], P[11], w0, w1, w2, nrm);
-  f.wnrm = {interp(P[12], P[15], P[18], w0, w1, w2, nrm), interp(P[13], P[16], P[19], w0, w1, w2, nrm),
-            interp(P[14], P[17], P[20], w0, w1, w2, nrm)};
-  f.wpos = {interp(P[21], P[24], P[27], w0, w1, w2, nrm), interp(P[22], P[25], P[28], w0, w1, w2, nrm),
-            interp(P[23], P[26], P[29], w0, w1, w2, nrm)};
-  return pack_rgb(fragment(v, f, prim), alpha_word);
-}
-
-__device__ __forceinline__ int payload_f4_r(int shader) {
-  switch (shader) {
-    case HSR_SHADER_FLAT: return 0;
-    case HSR_SHADER_SHADOW: case HSR_SHADER_GROUND: case HSR_SHADER_TOON: return 2;
-    case HSR_SHADER_TEXTURE: return 3;
-    case HSR_SHADER_TEXTURE_WITH_LIGHT: return 6;
-    default: return 8;
-  }
-}
+constexpr uint32_t kNone = 0xffffffffu;
 
 __device__ __forceinline__ int find_view(const DView* views, int nviews, int t) {
   int lo = 0, hi = nviews - 1;
@@ -121,6 +74,55 @@ __constant__ uint32_t kDivMagic[33] = {0,     65536, 32768, 21846, 16384, 13108,
                                        5958,  5462,  5042,  4682,  4370,  4096,  3856,  3641, 3450, 3277, 3121,
                                        2979,  2850,  2731,  2622,  2521,  2428,  2341,  2260, 2185, 2115, 2048};
 
+// Per-warp tile state in shared memory: key (ordered depth | submission), and for the
+// winner its payload index, seq and barycentric weights.
+template <int NPIX>
+struct TileState {
+  unsigned long long key[NPIX];
+  uint32_t pay[NPIX];
+  uint32_t seq[NPIX];
+  float b0[NPIX], b1[NPIX], b2[NPIX];
+};
+
+// Shade the winners of one tile and write colour, depth and prim id (fused clear writes the
+// clear values where nothing won).  S is the shader, known at compile time.
+template <int T, int S>
+__device__ __forceinline__ uint32_t shade_tile(const DView& v, const Scratch& sc, const TileState<T * T>& st, int ox,
+                                               int oy, bool clear, const ByteTables& bt) {
+  constexpr int PPL = T * T / 32;
+  constexpr int NF4 = payload_f4_of<S>();
+  const int lane = threadIdx.x & 31;
+  uint32_t shaded = 0;
+#pragma unroll 1
+  for (int q = 0; q < PPL; q++) {
+    const int p = lane + 32 * q;
+    const int x = ox + p % T, y = oy + p / T;
+    if (x >= v.W || y >= v.H) continue;
+    const size_t idx = (size_t)y * v.W + x;
+    const uint32_t pi = st.pay[p];
+    if (pi != kNone) {
+      shaded++;
+      float P[NF4 > 0 ? NF4 * 4 : 4];
+      if constexpr (NF4 > 0) {
+        const float4* src = reinterpret_cast<const float4*>(&sc.pay[pi]);
+#pragma unroll
+        for (int k = 0; k < NF4; k++) reinterpret_cast<float4*>(P)[k] = src[k];
+      }
+      const uint32_t seq = st.seq[p];
+      const uint32_t prim = v.prim_base + (seq >> 4) + 1u;
+      const uint32_t alpha = clear ? v.clear_rgba : __ldcg(&v.color[idx]);
+      v.color[idx] = pack_rgb(fragment_s<S>(v, P, st.b0[p], st.b1[p], st.b2[p], prim, bt), alpha);
+      v.depth[idx] = from_ord((uint32_t)(st.key[p] >> 32));
+      if (v.prim) v.prim[idx] = prim;
+    } else if (clear) {
+      v.color[idx] = v.clear_rgba;
+      v.depth[idx] = v.clear_depth;
+      if (v.prim) v.prim[idx] = 0u;
+    }
+  }
+  return shaded;
+}
+
 // One warp per screen tile.  For each batch of 32 records of the tile list, every record's
 // bounding-box pixels inside the tile form a run of candidates; the runs are laid end to
 // end (warp prefix sum) and the lanes walk the candidates 32 at a time, so the work is
@@ -128,20 +130,23 @@ __constant__ uint32_t kDivMagic[33] = {0,     65536, 32768, 21846, 16384, 13108,
 // A covered candidate resolves visibility with a 64-bit atomicMin on
 //     (ordered depth << 32) | (0xfffffffe - seq)
 // in shared memory: smallest depth first, and among equal depths the later submission.
-// The lane whose key is still the minimum after the warp's atomics records its record as
-// the pixel's winner (two lanes of one step never hold the same key: one triangle covers a
-// pixel once).  Shading then runs once per pixel with a winner.
+// The lane whose key is still the minimum after the warp's atomics records the winner's
+// payload, seq and weights (two lanes of one step never hold the same key: one triangle
+// covers a pixel once).  Shading then runs once per pixel with a winner.
 template <int T, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* __restrict__ views, Scratch sc) {
   constexpr int NPIX = T * T;
   constexpr int PPL = NPIX / 32;
-  __shared__ unsigned long long skey[WARPS][NPIX];
-  __shared__ uint32_t swin[WARPS][NPIX];
+  __shared__ TileState<NPIX> sst[WARPS];
   __shared__ RasterRec srec[WARPS][32];
-  __shared__ uint32_t sidx[WARPS][32];
   __shared__ uint32_t soff[WARPS][32];
   __shared__ uint32_t sbox[WARPS][32];
+  __shared__ float s_u8f[256], s_u8n[256];
+  build_byte_tables(s_u8f, s_u8n);
+  __syncthreads();
+  const ByteTables bt{s_u8f, s_u8n};
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  TileState<NPIX>& st = sst[warp];
   if (sc.ctl->error & kErrCapacity) return;
   const uint32_t nrec = min(sc.ctl->rec_count, sc.rec_cap);
 
@@ -189,8 +194,8 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
         const int x = ox + p % T, y = oy + p / T;
         float d = v.clear_depth;
         if (!clear && x < v.W && y < v.H) d = __ldcg(&v.depth[(size_t)y * v.W + x]);
-        skey[warp][p] = buffer_key(d);
-        swin[warp][p] = 0xffffffffu;
+        st.key[p] = buffer_key(d);
+        st.pay[p] = kNone;
       }
       for (uint32_t b = 0; b < n; b += 32) {
         const uint32_t cnt = min(32u, n - b);
@@ -202,7 +207,7 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
           if (ri < nrec) {
             rr = sc.recs[ri];
           } else {  // never produced by a consistent bin pass: covers nothing
-            rr.xr = 1u; rr.yr = 1u; rr.seq = 0u; rr.flags = 0u; rr.pad = 0u;
+            rr.xr = 1u; rr.yr = 1u; rr.seq = 0u; rr.view = 0u; rr.pad = kNone;
           }
           const int lx0 = max((int)(rr.xr & 0xffffu) - ox, 0), lx1 = min((int)(rr.xr >> 16) - ox, T - 1);
           const int ly0 = max((int)(rr.yr & 0xffffu) - oy, 0), ly1 = min((int)(rr.yr >> 16) - oy, T - 1);
@@ -211,7 +216,6 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
             sbox[warp][lane] = (uint32_t)lx0 | ((uint32_t)ly0 << 8) | ((uint32_t)(lx1 - lx0 + 1) << 16);
           }
           srec[warp][lane] = rr;
-          sidx[warp][lane] = ri;
         }
         uint32_t incl = c;
 #pragma unroll
@@ -227,6 +231,7 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
           bool covered = false;
           unsigned long long key = 0ull, old = 0ull;
           int p = 0, j = 0;
+          float b0 = 0.f, b1 = 0.f, b2 = 0.f;
           if (i < W) {
             // record j owning candidate i: the last j with soff[j] <= i (empty runs never win)
             int lo = 0, hi = (int)cnt - 1;
@@ -252,13 +257,12 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
             const float ux = fs(fm(r.e1x, dy), fm(dx, r.e1y));
             const float uy = fs(fm(dx, r.e2y), fm(r.e2x, dy));
             const float su = fa(ux, uy);
-            float b0, b1, b2;
-            if (!(r.flags & kRecExact)) {
+            if (!((r.view >> kRecFlagShift) & kRecExact)) {
               covered = (r.uz < 0.f) ? (su >= r.uz && uy <= 0.f && ux <= 0.f) : (su <= r.uz && uy >= 0.f && ux >= 0.f);
               if (covered) {
-                b0 = fs(1.f, fd(su, r.uz));
-                b1 = fd(uy, r.uz);
-                b2 = fd(ux, r.uz);
+                b0 = fs(1.f, div_m(su, r.uz, r.ruz));
+                b1 = div_m(uy, r.uz, r.ruz);
+                b2 = div_m(ux, r.uz, r.ruz);
               }
             } else {
               b0 = fs(1.f, fd(su, r.uz));
@@ -270,52 +274,34 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
               // interpolate_depth (graphics.cpp:186-194)
               const float z = fa(fa(fa(0.f, fm(r.d2, b2)), fm(r.d1, b1)), fm(r.d0, b0));
               key = ((unsigned long long)ord_bits(z) << 32) | (unsigned long long)(0xfffffffeu - r.seq);
-              old = atomicMin(&skey[warp][p], key);
+              old = atomicMin(&st.key[p], key);
             }
           }
           __syncwarp();
-          if (covered && old > key && skey[warp][p] == key) swin[warp][p] = sidx[warp][j];
+          if (covered && old > key && st.key[p] == key) {
+            const RasterRec& r = srec[warp][j];
+            st.pay[p] = r.pad;
+            st.seq[p] = r.seq;
+            st.b0[p] = b0;
+            st.b1[p] = b1;
+            st.b2[p] = b2;
+          }
           __syncwarp();
         }
       }
       __syncwarp();
       uint32_t shaded = 0;
-      const int nf4 = payload_f4_r(v.shader);
-#pragma unroll 1
-      for (int q = 0; q < PPL; q++) {
-        const int p = lane + 32 * q;
-        const int x = ox + p % T, y = oy + p / T;
-        if (x >= v.W || y >= v.H) continue;
-        const size_t idx = (size_t)y * v.W + x;
-        const uint32_t w = swin[warp][p];
-        if (w != 0xffffffffu) {
-          shaded++;
-          // the payload index equals the record index except for sub-records of a split
-          // triangle: load both at once, reload the payload in that rare case
-          const RasterRec r = sc.recs[w];
-          float P[kPayloadFloats];
-          {
-            float4* dst = reinterpret_cast<float4*>(P);
-            const float4* src = reinterpret_cast<const float4*>(&sc.pay[w]);
-#pragma unroll
-            for (int k = 0; k < kPayloadFloats / 4; k++)
-              dst[k] = k < nf4 ? src[k] : make_float4(0.f, 0.f, 0.f, 0.f);
-            if (r.pad != w) {
-              src = reinterpret_cast<const float4*>(&sc.pay[r.pad]);
-#pragma unroll
-              for (int k = 0; k < kPayloadFloats / 4; k++)
-                dst[k] = k < nf4 ? src[k] : make_float4(0.f, 0.f, 0.f, 0.f);
-            }
-          }
-          const uint32_t alpha = clear ? v.clear_rgba : __ldcg(&v.color[idx]);
-          v.color[idx] = shade_pixel(v, r, P, x, y, alpha);
-          v.depth[idx] = from_ord((uint32_t)(skey[warp][p] >> 32));
-          if (v.prim) v.prim[idx] = v.prim_base + (r.seq >> 4) + 1u;
-        } else if (clear) {
-          v.color[idx] = v.clear_rgba;
-          v.depth[idx] = v.clear_depth;
-          if (v.prim) v.prim[idx] = 0u;
-        }
+      switch (v.shader) {
+        case HSR_SHADER_GROUND: shaded = shade_tile<T, HSR_SHADER_GROUND>(v, sc, st, ox, oy, clear, bt); break;
+        case HSR_SHADER_TOON: shaded = shade_tile<T, HSR_SHADER_TOON>(v, sc, st, ox, oy, clear, bt); break;
+        case HSR_SHADER_TEXTURE: shaded = shade_tile<T, HSR_SHADER_TEXTURE>(v, sc, st, ox, oy, clear, bt); break;
+        case HSR_SHADER_TEXTURE_WITH_LIGHT:
+          shaded = shade_tile<T, HSR_SHADER_TEXTURE_WITH_LIGHT>(v, sc, st, ox, oy, clear, bt);
+          break;
+        case HSR_SHADER_BLINN: shaded = shade_tile<T, HSR_SHADER_BLINN>(v, sc, st, ox, oy, clear, bt); break;
+        case HSR_SHADER_NORMALMAP: shaded = shade_tile<T, HSR_SHADER_NORMALMAP>(v, sc, st, ox, oy, clear, bt); break;
+        case HSR_SHADER_SHADOW: shaded = shade_tile<T, HSR_SHADER_SHADOW>(v, sc, st, ox, oy, clear, bt); break;
+        default: shaded = shade_tile<T, HSR_SHADER_FLAT>(v, sc, st, ox, oy, clear, bt); break;
       }
       shaded = __reduce_add_sync(kFull, shaded);
       if (lane == 0 && shaded) atomicAdd(&sc.ctl->shaded_px, (unsigned long long)shaded);
@@ -340,9 +326,46 @@ int launch_raster(const DView* views, int tile, Scratch sc, int grid, int warps,
   if (warps != 4 && warps != 8) return (int)cudaErrorInvalidValue;
   switch (tile) {
     case 8: return warps == 4 ? launch_t<8, 4>(views, sc, grid, s) : launch_t<8, 8>(views, sc, grid, s);
-    case 16: return warps == 4 ? launch_t<16, 4>(views, sc, grid, s) : launch_t<16, 8>(views, sc, grid, s);
+    case 16: return warps == 4 ? launch_t<16, 4>(views, sc, grid, s) : (int)cudaErrorInvalidValue;
     default: return (int)cudaErrorInvalidValue;
   }
+}
+
+// ---- self-test of the division used by the raster ----------------------------------------
+// Compares div_m against __fdiv_rn on (a, b) pairs from a counter-based generator over the
+// magnitudes the raster divides (|b| in [2^-7, 2^30], quotients from 2^-110 to 2^12,
+// including zero, powers of two and all-ones mantissas), and counts the pairs whose bits
+// differ.
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {
+  x ^= x >> 30; x *= 0xbf58476d1ce4e5b9ull;
+  x ^= x >> 27; x *= 0x94d049bb133111ebull;
+  return x ^ (x >> 31);
+}
+
+__global__ void k_selftest_div(uint64_t n, uint64_t seed, unsigned long long* mismatches) {
+  unsigned long long local = 0;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t h = mix64(seed ^ (i * 0x9e3779b97f4a7c15ull));
+    const int eb = (int)(h & 63u) % 38 - 7;                // exponent of b in [-7, 30]
+    const int ea = eb + (int)((h >> 6) & 127u) % 122 - 110;  // a from b - 110 to b + 11 binades
+    uint32_t mb = (uint32_t)(h >> 12) & 0x7fffffu, ma = (uint32_t)(h >> 35) & 0x7fffffu;
+    if (((h >> 58) & 7u) == 0) mb = 0;          // powers of two
+    if (((h >> 61) & 7u) == 1) ma = 0x7fffffu;  // all-ones mantissas
+    float b = __uint_as_float(((uint32_t)(eb + 127) << 23) | mb);
+    float a = __uint_as_float(((uint32_t)(max(ea, -126) + 127) << 23) | ma);
+    if ((h >> 63) & 1u) b = -b;
+    if ((h >> 62) & 1u) a = -a;
+    if (((h >> 56) & 63u) == 7) a = 0.f;
+    const float ref = __fdiv_rn(a, b);
+    const float got = div_m(a, b, __frcp_rn(b));
+    if (__float_as_uint(ref) != __float_as_uint(got)) local++;
+  }
+  if (local) atomicAdd(mismatches, local);
+}
+
+int launch_selftest_div(uint64_t n, uint64_t seed, unsigned long long* mismatches, cudaStream_t s) {
+  k_selftest_div<<<1024, 256, 0, s>>>(n, seed, mismatches);
+  return (int)cudaGetLastError();
 }
 
 }  // namespace hsr
