@@ -74,24 +74,6 @@ __device__ __forceinline__ Col c_mulf(Col a, float t) {
 __device__ __forceinline__ Col c_mulc(Col a, Col b) { return {fm(a.r, b.r), fm(a.g, b.g), fm(a.b, b.b), fm(a.a, b.a)}; }
 __device__ __forceinline__ Col c_of(const float* p) { return {p[0], p[1], p[2], p[3]}; }
 
-// ---- division --------------------------------------------------------------------------
-// a / b rounded to nearest, given y = RN(1/b) (__frcp_rn), by Markstein's theorem
-// (P. Markstein, IBM J. Res. Dev. 34(1), 1990; also Muller et al., Handbook of
-// Floating-Point Arithmetic, the "Markstein iteration"): if y is the correctly rounded
-// reciprocal and q is within one ulp of a/b, the remainder r = a - b*q is exact in an FMA
-// and RN(q + r*y) is the correctly rounded quotient.  One refinement step brings
-// q0 = RN(a*y) (within two ulps) within one ulp, the second step rounds correctly.  Valid
-// while no intermediate overflows or underflows, which the raster guarantees by routing
-// records outside its coordinate range to the literal division (kRecExact).  A device
-// self-test compares it with __fdiv_rn (hsr_selftest).
-__device__ __forceinline__ float div_m(float a, float b, float y) {
-  float q = __fmul_rn(a, y);
-  float r = __fmaf_rn(-b, q, a);
-  q = __fmaf_rn(r, y, q);
-  r = __fmaf_rn(-b, q, a);
-  return __fmaf_rn(r, y, q);
-}
-
 // ---- byte -> float tables --------------------------------------------------------------
 // Colour channels and normal-map components are bytes; their float values are the IEEE
 // results b/255.f (color.cpp:5, renderbuffer.cpp:46) and (b/255.f)*2.f - 1.f

@@ -51,7 +51,7 @@ struct __align__(16) RasterRec {
   uint32_t seq;             // (face << 4) | (fan << 1) | clipped — submission order
   uint32_t view;            // index of the view in the batch | flags << 28 (kRec*)
   uint32_t xr, yr;          // inclusive pixel range: x0 | x1 << 16, y0 | y1 << 16
-  float ruz;                // RN(1 / uz), for the division of the depth weights
+  uint32_t rsv;             // reserved (zero)
   uint32_t pad;             // payload index
 };
 constexpr uint32_t kRecViewMask = 0x0fffffffu;
@@ -154,6 +154,5 @@ int launch_scan(Scratch sc, cudaStream_t s);
 int launch_scatter(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s);
 int launch_raster(const DView* views, int tile, Scratch sc, int grid, int warps, cudaStream_t s);
 int scan_blocks(int ntiles);
-int launch_selftest_div(uint64_t n, uint64_t seed, unsigned long long* mismatches, cudaStream_t s);
 
 }  // namespace hsr

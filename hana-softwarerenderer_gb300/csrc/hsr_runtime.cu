@@ -811,23 +811,6 @@ int hsr_autotune(const hsr_draw_desc* descs, int32_t n, int32_t reps, hsr_tuning
   return HSR_OK;
 }
 
-int hsr_selftest_division(uint64_t n, uint64_t seed, uint64_t* mismatches) {
-  RT_OR_FAIL();
-  if (!mismatches) return fail(HSR_ERR_INVALID_ARG, "selftest_division: null");
-  unsigned long long* d = nullptr;
-  int rc = g_rt->arena.reserve(sizeof(unsigned long long));
-  if (rc != HSR_OK) return rc;
-  d = reinterpret_cast<unsigned long long*>(g_rt->arena.base);
-  cudaError_t e = cudaMemsetAsync(d, 0, sizeof(*d), g_rt->stream);
-  if (e == cudaSuccess) e = (cudaError_t)launch_selftest_div(n, seed, d, g_rt->stream);
-  unsigned long long h = 0;
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, g_rt->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(g_rt->stream);
-  if (e != cudaSuccess) return cuda_fail(e, "selftest_division");
-  *mismatches = h;
-  return HSR_OK;
-}
-
 int hsr_get_stats(hsr_stats* out) {
   RT_OR_FAIL();
   if (!out) return fail(HSR_ERR_INVALID_ARG, "get_stats: null");

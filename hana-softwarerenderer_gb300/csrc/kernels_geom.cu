@@ -120,7 +120,7 @@ __device__ __forceinline__ bool build_rec(const DView& v, float4 c0, float4 c1, 
   const bool ok = coord_ok(s0.x) && coord_ok(s0.y) && coord_ok(s1.x) && coord_ok(s1.y) &&
                   coord_ok(s2.x) && coord_ok(s2.y) && fabsf(uz) <= 0x1p30f;
   r.view = view | ((ok ? 0u : kRecExact) << kRecFlagShift);
-  r.ruz = __frcp_rn(uz);
+  r.rsv = 0u;
   r.pad = 0u;
   return true;
 }

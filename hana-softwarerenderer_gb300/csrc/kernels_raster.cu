@@ -19,7 +19,7 @@
 // so the test needs no division.  The equivalence holds when nonzero |ux|, |uy| cannot
 // underflow after the division; setup marks records outside that range (kRecExact) and
 // those evaluate the reference's divisions literally.  Covered pixels then compute the
-// three quotients exactly for the depth (div_m with the record's RN(1/uz)).
+// three IEEE quotients for the depth.
 #include <float.h>
 
 #include "hsr_device.cuh"
@@ -260,9 +260,9 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
             if (!((r.view >> kRecFlagShift) & kRecExact)) {
               covered = (r.uz < 0.f) ? (su >= r.uz && uy <= 0.f && ux <= 0.f) : (su <= r.uz && uy >= 0.f && ux >= 0.f);
               if (covered) {
-                b0 = fs(1.f, div_m(su, r.uz, r.ruz));
-                b1 = div_m(uy, r.uz, r.ruz);
-                b2 = div_m(ux, r.uz, r.ruz);
+                b0 = fs(1.f, fd(su, r.uz));
+                b1 = fd(uy, r.uz);
+                b2 = fd(ux, r.uz);
               }
             } else {
               b0 = fs(1.f, fd(su, r.uz));
@@ -329,43 +329,6 @@ int launch_raster(const DView* views, int tile, Scratch sc, int grid, int warps,
     case 16: return warps == 4 ? launch_t<16, 4>(views, sc, grid, s) : (int)cudaErrorInvalidValue;
     default: return (int)cudaErrorInvalidValue;
   }
-}
-
-// ---- self-test of the division used by the raster ----------------------------------------
-// Compares div_m against __fdiv_rn on (a, b) pairs from a counter-based generator over the
-// magnitudes the raster divides (|b| in [2^-7, 2^30], quotients from 2^-110 to 2^12,
-// including zero, powers of two and all-ones mantissas), and counts the pairs whose bits
-// differ.
-__device__ __forceinline__ uint64_t mix64(uint64_t x) {
-  x ^= x >> 30; x *= 0xbf58476d1ce4e5b9ull;
-  x ^= x >> 27; x *= 0x94d049bb133111ebull;
-  return x ^ (x >> 31);
-}
-
-__global__ void k_selftest_div(uint64_t n, uint64_t seed, unsigned long long* mismatches) {
-  unsigned long long local = 0;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t h = mix64(seed ^ (i * 0x9e3779b97f4a7c15ull));
-    const int eb = (int)(h & 63u) % 38 - 7;                // exponent of b in [-7, 30]
-    const int ea = eb + (int)((h >> 6) & 127u) % 122 - 110;  // a from b - 110 to b + 11 binades
-    uint32_t mb = (uint32_t)(h >> 12) & 0x7fffffu, ma = (uint32_t)(h >> 35) & 0x7fffffu;
-    if (((h >> 58) & 7u) == 0) mb = 0;          // powers of two
-    if (((h >> 61) & 7u) == 1) ma = 0x7fffffu;  // all-ones mantissas
-    float b = __uint_as_float(((uint32_t)(eb + 127) << 23) | mb);
-    float a = __uint_as_float(((uint32_t)(max(ea, -126) + 127) << 23) | ma);
-    if ((h >> 63) & 1u) b = -b;
-    if ((h >> 62) & 1u) a = -a;
-    if (((h >> 56) & 63u) == 7) a = 0.f;
-    const float ref = __fdiv_rn(a, b);
-    const float got = div_m(a, b, __frcp_rn(b));
-    if (__float_as_uint(ref) != __float_as_uint(got)) local++;
-  }
-  if (local) atomicAdd(mismatches, local);
-}
-
-int launch_selftest_div(uint64_t n, uint64_t seed, unsigned long long* mismatches, cudaStream_t s) {
-  k_selftest_div<<<1024, 256, 0, s>>>(n, seed, mismatches);
-  return (int)cudaGetLastError();
 }
 
 }  // namespace hsr

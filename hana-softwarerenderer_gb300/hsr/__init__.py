@@ -104,7 +104,6 @@ def lib():
                          ctypes.c_int),
         "hsr_last_timing": ([ctypes.POINTER(Timing)], ctypes.c_int),
         "hsr_host_alloc": ([ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
-        "hsr_selftest_division": ([ctypes.c_uint64, ctypes.c_uint64, _u64p], ctypes.c_int),
         "hsr_host_free": ([ctypes.c_void_p], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
@@ -157,13 +156,6 @@ def autotune(descs, reps: int = 3) -> dict:
     t = Tuning()
     check(lib().hsr_autotune(arr, len(descs), reps, ctypes.byref(t)))
     return {k: getattr(t, k) for k, _ in Tuning._fields_}
-
-
-def selftest_division(n: int, seed: int = 1) -> int:
-    """Bits-differ count of the raster's division against IEEE division on n pairs."""
-    m = ctypes.c_uint64()
-    check(lib().hsr_selftest_division(n, seed, ctypes.byref(m)))
-    return int(m.value)
 
 
 def stats() -> dict:

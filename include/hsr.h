@@ -205,12 +205,6 @@ typedef struct hsr_timing {
 HSR_API int hsr_set_profiling(int on);
 HSR_API int hsr_last_timing(hsr_timing* out);
 
-/* Diagnostics: the raster divides by a triangle's u.z through its correctly rounded
- * reciprocal (Markstein's theorem) instead of an IEEE division per quotient.  This runs
- * n seeded (a, b) pairs over the raster's magnitude range through both and reports how
- * many results differ in any bit (0 expected). */
-HSR_API int hsr_selftest_division(uint64_t n, uint64_t seed, uint64_t* mismatches);
-
 /* Page-locked host memory for buffers passed to upload / download (fast DMA). */
 HSR_API int hsr_host_alloc(size_t bytes, void** out);
 HSR_API int hsr_host_free(void* p);

@@ -238,12 +238,3 @@ def test_autotune_picks_a_valid_config_and_stays_exact(gpu):
         gpu.set_tuning(tile=old.tile, warps_per_cta=old.warps_per_cta, ctas_per_sm=old.ctas_per_sm,
                        bin_factor=old.bin_factor)
     assert_parity(got, exp, f"autotuned {best}")
-
-
-def test_raster_division_matches_ieee_division(gpu):
-    """The raster's depth weights divide by u.z through RN(1/u.z) and two Markstein steps;
-    every quotient must equal the IEEE division bit for bit."""
-    import hsr
-
-    assert hsr.selftest_division(1 << 28, seed=1) == 0
-    assert hsr.selftest_division(1 << 28, seed=2) == 0
