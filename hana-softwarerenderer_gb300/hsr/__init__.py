@@ -95,6 +95,7 @@ def lib():
         "hsr_target_download": ([ctypes.c_uint64, _u8p, _f32p, _u32p], ctypes.c_int),
         "hsr_draw": ([ctypes.POINTER(DrawDesc)], ctypes.c_int),
         "hsr_draw_batch": ([ctypes.POINTER(DrawDesc), ctypes.c_int32], ctypes.c_int),
+        "hsr_draw_noalloc": ([ctypes.POINTER(DrawDesc)], ctypes.c_int),
         "hsr_synchronize": ([], ctypes.c_int),
         "hsr_get_tuning": ([ctypes.POINTER(Tuning)], ctypes.c_int),
         "hsr_set_tuning": ([ctypes.POINTER(Tuning)], ctypes.c_int),
@@ -309,6 +310,11 @@ def make_desc(mesh: Mesh, shader: int, sd: np.ndarray, target: Target, diffuse: 
 
 def draw(desc: DrawDesc) -> None:
     check(lib().hsr_draw(ctypes.byref(desc)))
+
+
+def draw_noalloc(desc: DrawDesc) -> None:
+    """hsr_draw_noalloc: the draw on the library's fixed 128 MiB scratch, no allocation."""
+    check(lib().hsr_draw_noalloc(ctypes.byref(desc)))
 
 
 def draw_batch(descs) -> None:

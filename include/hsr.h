@@ -157,6 +157,20 @@ HSR_API int hsr_draw(const hsr_draw_desc* desc);
 HSR_API int hsr_draw_batch(const hsr_draw_desc* descs, int32_t n);
 HSR_API int hsr_synchronize(void);
 
+/* hsr_draw_noalloc: the same draw as hsr_draw, for callers that must not allocate while
+ * drawing — work recorded into a CUDA graph (allocation is not allowed during stream
+ * capture), real-time loops that cannot stall on cudaMalloc's device-wide
+ * synchronisation, and processes held to a fixed device-memory budget.  It has no
+ * counterpart in the reference.  Meshes, textures and targets are the caller's existing
+ * handles; the call's own scratch is one fixed 128 MiB device array that every GPU loading
+ * this library holds until exit, so it calls no cudaMalloc, cudaFree or cudaMallocHost.
+ * A draw needing more than 128 MiB of scratch is refused with HSR_ERR_INVALID_ARG (roughly
+ * 400k faces into 1920x1080); one that overflows the fixed split on the device returns
+ * HSR_ERR_BIN_OVERFLOW with the target untouched.  All calls share the array: calls whose
+ * GPU work overlaps race, so issue them one after another.  The first call on a device
+ * looks up the array's address on that device; make it before any stream capture. */
+HSR_API int hsr_draw_noalloc(const hsr_draw_desc* desc);
+
 /* ---- tuning ------------------------------------------------------------------------- */
 typedef struct hsr_tuning {
   int32_t tile;           /* raster tile edge in pixels: 8 or 16                    */
