@@ -162,6 +162,15 @@ def kernel_bytes(t: dict) -> dict:
     }
 
 
+def ncu_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu capture of this workload."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        return json.load(f)["dram_bytes_per_launch"].get(kernel)
+
+
 def run_ours(args, world, rank, local):
     import torch
 
@@ -244,7 +253,7 @@ def run_ours(args, world, rank, local):
     roof = {"kernel": top, "bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"],
             "peak_source": pk["source"], "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4),
             "algorithmic_bytes": int(kb[top]), "ms": round(mean_k[top], 5),
-            "traffic": args.traffic_bytes if args.traffic_bytes else None,
+            "traffic": args.traffic_bytes if args.traffic_bytes else ncu_traffic(top),
             "share": {k: round(v / sum(mean_k.values()), 4) for k, v in mean_k.items()}}
 
     out = {
