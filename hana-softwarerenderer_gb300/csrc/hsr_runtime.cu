@@ -77,9 +77,8 @@ TexObj::~TexObj() {
   if (words) cudaFree(words);
 }
 TargetObj::~TargetObj() {
-  if (color) cudaFree(color);
-  if (depth) cudaFree(depth);
-  if (prim) cudaFree(prim);
+  if (pooled || !block) return;
+  cudaFreeAsync(block, stream);
 }
 
 int Arena::reserve(size_t bytes) {
@@ -339,7 +338,9 @@ int Plan::enqueue(cudaStream_t s, int num_sms, const hsr_tuning& tu, cudaEvent_t
   kr = launch_scan(sc, s);
   if (kr) return cuda_fail((cudaError_t)kr, "scan kernel");
   if (ev && ev[4]) cudaEventRecord(ev[4], s);
-  kr = launch_scatter(dviews, tile, sc, (int)std::max<size_t>((rec_cap + 255) / 256, 1), s);
+  // grid-stride over the records: a full-occupancy grid, not one sized by the capacity
+  // (which can be far above this batch's record count)
+  kr = launch_scatter(dviews, tile, sc, (int)std::max<size_t>(std::min<size_t>((rec_cap + 255) / 256, (size_t)num_sms * 8), 1), s);
   if (kr) return cuda_fail((cudaError_t)kr, "scatter kernel");
   if (ev && ev[5]) cudaEventRecord(ev[5], s);
   kr = launch_raster(dviews, tile, sc, num_sms * tu.ctas_per_sm, tu.warps_per_cta, s);
@@ -484,6 +485,12 @@ int hsr_init(int device) {
   e = cudaGetDeviceProperties(&prop, device);
   if (e != cudaSuccess) { delete rt; return cuda_fail(e, "cudaGetDeviceProperties"); }
   rt->num_sms = prop.multiProcessorCount;
+  // keep memory freed into the device's stream-ordered pool cached instead of returning it
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
   e = cudaStreamCreateWithFlags(&rt->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { delete rt; return cuda_fail(e, "cudaStreamCreate"); }
   for (int k = 0; k < 7; k++) {
@@ -495,6 +502,7 @@ int hsr_init(int device) {
 }
 
 int hsr_shutdown(void) {
+  serve_shutdown();
   std::lock_guard<std::mutex> lock(g_mu);
   if (!g_rt) return HSR_OK;
   cudaStreamSynchronize(g_rt->stream);
@@ -637,10 +645,20 @@ int hsr_target_create(int32_t w, int32_t h, hsr_target* out) {
   TargetObj* t = new TargetObj();
   t->w = w; t->h = h;
   const size_t n = (size_t)w * (size_t)h;
-  int rc = dalloc((void**)&t->color, 4 * n, "target colour");
-  if (rc == HSR_OK) rc = dalloc((void**)&t->depth, 4 * n, "target depth");
-  if (rc == HSR_OK) rc = dalloc((void**)&t->prim, 4 * n, "target prim ids");
-  if (rc != HSR_OK) { delete t; return rc; }
+  // the three planes in one block from the device's stream-ordered pool (freed blocks stay
+  // cached in the pool, so creating and releasing targets of varying size stays cheap)
+  const size_t plane = align_up(4 * n, 256);
+  cudaError_t e = cudaMallocAsync((void**)&t->block, 3 * plane, g_rt->stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    t->block = nullptr;
+    delete t;
+    return fail(HSR_ERR_OUT_OF_MEMORY, "target: device allocation of " + std::to_string(3 * plane) + " bytes failed");
+  }
+  t->stream = g_rt->stream;
+  t->color = reinterpret_cast<uint32_t*>(t->block);
+  t->depth = reinterpret_cast<float*>(t->block + plane);
+  t->prim = reinterpret_cast<uint32_t*>(t->block + 2 * plane);
   // RenderBuffer's constructor clears to colour (0,0,0,1) -> bytes (0,0,0,255) and depth 1
   // (renderbuffer.cpp:3-18)
   const uint8_t rgba[4] = {0, 0, 0, 255};

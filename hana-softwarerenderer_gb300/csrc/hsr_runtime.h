@@ -32,6 +32,9 @@ struct TargetObj {  // RenderBuffer (renderbuffer.h:5-22) + prim-id plane
   float* depth = nullptr;
   uint32_t* prim = nullptr;
   int32_t w = 0, h = 0;
+  char* block = nullptr;          // one stream-ordered allocation holding the three planes
+  cudaStream_t stream = nullptr;  // the stream it was allocated on (and is freed on)
+  bool pooled = false;  // memory owned by a server's pool (freed by the server, not here)
   ~TargetObj();
 };
 
@@ -110,6 +113,7 @@ extern thread_local std::string g_last_error;
 int fail(int code, const std::string& msg);
 int cuda_fail(cudaError_t e, const char* where);
 void mat_mul_ref(const float* a, const float* b, float* out);
+void serve_shutdown();
 int launch_clear(uint32_t* color, float* depth, uint32_t* prim, size_t n, uint32_t rgba, float d, cudaStream_t s);
 
 }  // namespace hsr

@@ -240,6 +240,23 @@ __device__ __forceinline__ bool vertex_visible(float4 c) {  // is_vertex_visible
   return fabsf(c.x) <= c.w && fabsf(c.y) <= c.w && fabsf(c.z) <= c.w;
 }
 
+// True when the reference's clipper returns 0 vertices for this face without creating any
+// new vertex: Sutherland-Hodgman copies a polygon whose vertices are all inside a plane
+// unchanged, so if the three corners pass every plane before some plane (in the order
+// W, +X, -X, +Y, -Y, +Z, -Z of graphics.cpp:152-158) and all fail that plane, that stage
+// emits nothing and the face is dropped (CLIP_IN2OUT / CLIP_OUT2IN return 0).  Faces whose
+// corners straddle a plane first go to the full clipper.
+__device__ __forceinline__ bool clip_trivially_empty(float4 c0, float4 c1, float4 c2) {
+  const float a[4] = {c0.x, c0.y, c0.z, c0.w}, b[4] = {c1.x, c1.y, c1.z, c1.w}, c[4] = {c2.x, c2.y, c2.z, c2.w};
+#pragma unroll
+  for (int plane = PW; plane <= NZ; plane++) {
+    const bool ia = inside_plane(a, plane), ib = inside_plane(b, plane), ic = inside_plane(c, plane);
+    if (!ia && !ib && !ic) return true;
+    if (!(ia && ib && ic)) return false;
+  }
+  return false;
+}
+
 constexpr int kSetupThreads = 256;
 constexpr int kPolyStride = kVaryings;  // floats per polygon vertex in shared memory
 
@@ -293,7 +310,7 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const DView* __restrict
         make_payload(v.shader, c[0], c[1], c[2], pl);
       }
     } else {
-      needs_clip = true;
+      needs_clip = !clip_trivially_empty(c0, c1, c2);
     }
   }
   int tx0, ty0, ntw, nt = 0;

@@ -62,6 +62,25 @@ class Stats(ctypes.Structure):
                 ("tiles", ctypes.c_uint64), ("retries", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("pool_bytes", ctypes.c_uint64), ("max_batch", ctypes.c_int32), ("slots", ctypes.c_int32)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("mesh", ctypes.c_uint64), ("shader", ctypes.c_int32), ("diffuse", ctypes.c_uint64),
+                ("normal", ctypes.c_uint64), ("width", ctypes.c_int32), ("height", ctypes.c_int32),
+                ("shadow_size", ctypes.c_int32), ("uniforms", ctypes.c_float * 121),
+                ("clear_rgba", ctypes.c_uint8 * 4), ("clear_depth", ctypes.c_float),
+                ("shadow_clear_rgba", ctypes.c_uint8 * 4), ("shadow_clear_depth", ctypes.c_float),
+                ("out_rgba", ctypes.c_void_p), ("out_depth", ctypes.c_void_p), ("out_prim", ctypes.c_void_p)]
+
+
+class RequestStatus(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("batch", ctypes.c_uint32), ("batch_requests", ctypes.c_uint32),
+                ("pad", ctypes.c_uint32), ("submit_ms", ctypes.c_double), ("launch_ms", ctypes.c_double),
+                ("done_ms", ctypes.c_double)]
+
+
 _lib = None
 
 
@@ -106,6 +125,18 @@ def lib():
         "hsr_last_timing": ([ctypes.POINTER(Timing)], ctypes.c_int),
         "hsr_host_alloc": ([ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
         "hsr_host_free": ([ctypes.c_void_p], ctypes.c_int),
+        "hsr_plan_create": ([ctypes.POINTER(DrawDesc), ctypes.c_int32, _u64p], ctypes.c_int),
+        "hsr_plan_set_uniforms": ([ctypes.c_uint64, ctypes.c_int32, ctypes.c_void_p], ctypes.c_int),
+        "hsr_plan_launch": ([ctypes.c_uint64], ctypes.c_int),
+        "hsr_plan_wait": ([ctypes.c_uint64], ctypes.c_int),
+        "hsr_plan_release": ([ctypes.c_uint64], ctypes.c_int),
+        "hsr_server_create": ([ctypes.POINTER(ServerConfig), _u64p], ctypes.c_int),
+        "hsr_server_submit": ([ctypes.c_uint64, ctypes.POINTER(Request), _u64p], ctypes.c_int),
+        "hsr_server_poll": ([ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(RequestStatus)], ctypes.c_int),
+        "hsr_server_wait": ([ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int32, ctypes.POINTER(RequestStatus)],
+                            ctypes.c_int),
+        "hsr_server_now_ms": ([ctypes.c_uint64, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+        "hsr_server_destroy": ([ctypes.c_uint64], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -320,3 +351,111 @@ def draw_noalloc(desc: DrawDesc) -> None:
 def draw_batch(descs) -> None:
     arr = (DrawDesc * len(descs))(*descs)
     check(lib().hsr_draw_batch(arr, len(descs)))
+
+
+class Plan:
+    """A batch recorded once into a CUDA graph (hsr_plan_create) and replayed; only the
+    uniforms of its draws change between replays."""
+
+    def __init__(self, descs):
+        arr = (DrawDesc * len(descs))(*descs)
+        h = ctypes.c_uint64()
+        check(lib().hsr_plan_create(arr, len(descs), ctypes.byref(h)))
+        self.handle = h.value
+        self.n = len(descs)
+
+    def set_uniforms(self, draw: int, sd) -> None:
+        sdb = np.ascontiguousarray(np.asarray(sd, dtype=SHADER_DATA_DTYPE).reshape(()))
+        check(lib().hsr_plan_set_uniforms(self.handle, draw, sdb.ctypes.data))
+
+    def launch(self) -> None:
+        check(lib().hsr_plan_launch(self.handle))
+
+    def wait(self) -> None:
+        check(lib().hsr_plan_wait(self.handle))
+
+    def release(self) -> None:
+        if self.handle:
+            check(lib().hsr_plan_release(self.handle))
+            self.handle = 0
+
+
+_FLT_MAX = float(np.finfo(np.float32).max)
+
+
+class Server:
+    """Continuous-batching render server (hsr_server_*): requests are queued, admitted while
+    the framebuffer pool has room, batched into launch sequences on `slots` streams, and their
+    colour / depth / prim ids copied into the arrays given at submission."""
+
+    def __init__(self, pool_bytes: int, max_batch: int = 64, slots: int = 2):
+        cfg = ServerConfig(pool_bytes, max_batch, slots)
+        h = ctypes.c_uint64()
+        check(lib().hsr_server_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self.handle = h.value
+        self._live: dict[int, tuple] = {}
+
+    def submit(self, mesh: Mesh, shader: int, sd, width: int, height: int, diffuse: Texture | None = None,
+               normal: Texture | None = None, shadow_size: int = 0, clear=((0, 0, 0, 255), _FLT_MAX),
+               shadow_clear=((0, 0, 0, 255), _FLT_MAX), out: dict | None = None) -> int:
+        """`out` may hold "color" (h,w,4) u8, "depth" (h,w) f32 and "prim" (h,w) u32 arrays
+        (page-locked ones keep the copies asynchronous); they stay referenced until the
+        request is waited for."""
+        out = out or {}
+        r = Request()
+        r.mesh = mesh.handle
+        r.shader = shader
+        r.diffuse = diffuse.handle if diffuse else 0
+        r.normal = normal.handle if normal else 0
+        r.width, r.height, r.shadow_size = width, height, shadow_size
+        sdb = np.ascontiguousarray(np.asarray(sd, dtype=SHADER_DATA_DTYPE).reshape(()))
+        ctypes.memmove(ctypes.addressof(r.uniforms), sdb.ctypes.data, SHADER_DATA_DTYPE.itemsize)
+        for i in range(4):
+            r.clear_rgba[i] = clear[0][i]
+            r.shadow_clear_rgba[i] = shadow_clear[0][i]
+        r.clear_depth = float(clear[1])
+        r.shadow_clear_depth = float(shadow_clear[1])
+        arrays = []
+        for key, field, dt, shape in (("color", "out_rgba", np.uint8, (height, width, 4)),
+                                      ("depth", "out_depth", np.float32, (height, width)),
+                                      ("prim", "out_prim", np.uint32, (height, width))):
+            a = out.get(key)
+            if a is not None:
+                if a.dtype != dt or a.shape != shape or not a.flags.c_contiguous or not a.flags.writeable:
+                    raise ValueError(f"out[{key!r}] must be a writeable contiguous {np.dtype(dt).name} {shape}")
+                setattr(r, field, a.ctypes.data)
+                arrays.append(a)
+        t = ctypes.c_uint64()
+        check(lib().hsr_server_submit(self.handle, ctypes.byref(r), ctypes.byref(t)))
+        self._live[t.value] = tuple(arrays)
+        return t.value
+
+    @staticmethod
+    def _status(st: RequestStatus) -> dict:
+        return {k: getattr(st, k) for k, _ in RequestStatus._fields_ if k != "pad"}
+
+    def poll(self, ticket: int) -> dict | None:
+        st = RequestStatus()
+        rc = lib().hsr_server_poll(self.handle, ticket, ctypes.byref(st))
+        if rc == ERR_BUSY:
+            return None
+        check(rc)
+        self._live.pop(ticket, None)
+        return self._status(st)
+
+    def wait(self, ticket: int, timeout_ms: int = 120000) -> dict:
+        st = RequestStatus()
+        check(lib().hsr_server_wait(self.handle, ticket, timeout_ms, ctypes.byref(st)))
+        self._live.pop(ticket, None)
+        return self._status(st)
+
+    def now_ms(self) -> float:
+        v = ctypes.c_double()
+        check(lib().hsr_server_now_ms(self.handle, ctypes.byref(v)))
+        return v.value
+
+    def close(self) -> None:
+        if self.handle:
+            check(lib().hsr_server_destroy(self.handle))
+            self.handle = 0
+            self._live.clear()

@@ -324,6 +324,134 @@ def soup_frame(ntri: int = 4_000_000, width: int = 3840, height: int = 2160, see
     return Frame(mesh, FLAT, sd, width, height, name=f"soup{ntri}_{width}x{height}")
 
 
+# ---------------------------------------------------------------------------------
+# batched views and serving
+# ---------------------------------------------------------------------------------
+# hsr_shader_kind values a request may ask for (the reference scenes' shaders)
+REQUEST_SHADERS = (GROUND, TOON, TEXTURE, TEXTURE_WITH_LIGHT, BLINN, NORMALMAP)
+
+
+@dataclasses.dataclass
+class PoolMesh:
+    mesh: Mesh
+    kind: str          # "sphere" | "grid"
+    name: str
+
+
+def pool_mesh(kind: str, size: int, seed: int) -> PoolMesh:
+    """A displaced icosphere of subdivision `size` (20*4^size triangles) or a height-field
+    grid of size x size cells (2*size^2 triangles)."""
+    if kind == "sphere":
+        return PoolMesh(sphere_mesh(size, displace=0.05, seed=seed), kind, f"ico{size}_s{seed}")
+    return PoolMesh(grid_mesh(size, size, seed), kind, f"grid{size}_s{seed}")
+
+
+# 8 meshes from 2,048 to 1,310,720 triangles (roughly geometric)
+VIEW_POOL_SPEC = (("grid", 32), ("sphere", 4), ("sphere", 5), ("grid", 128),
+                  ("sphere", 6), ("grid", 256), ("sphere", 7), ("sphere", 8))
+# 16 meshes, 8,257,536 triangles in total
+SERVE_POOL_SPEC = (("sphere", 8),) * 3 + (("sphere", 7),) * 6 + (("grid", 512),) * 4 + (("sphere", 6),) * 3
+
+
+def mesh_pool(spec, seed: int) -> list:
+    return [pool_mesh(kind, size, seed + 101 * i) for i, (kind, size) in enumerate(spec)]
+
+
+def orbit_eye(rng: np.random.Generator, kind: str) -> tuple:
+    """Random orbit camera around the origin at radius 2-4; grids are seen from above
+    (their triangles face +y)."""
+    r = rng.uniform(2.0, 4.0)
+    az = rng.uniform(0, 2 * np.pi)
+    el = rng.uniform(0.35, 1.1) if kind == "grid" else rng.uniform(-0.6, 1.0)
+    return (float(r * math.cos(el) * math.sin(az)), float(r * math.sin(el)), float(r * math.cos(el) * math.cos(az)))
+
+
+@dataclasses.dataclass
+class View:
+    """One DrawModel::draw on a pooled mesh: which mesh / textures, target size, shader,
+    uniforms and shadow map size (0: no shadow pass)."""
+    mesh: int
+    tex: int
+    shader: int
+    width: int
+    height: int
+    shadow: int
+    sd: np.ndarray
+
+
+def view_set(pool: list, n: int = 64, seed: int = 3, ntex: int = 4) -> list:
+    """64 views: resolution uniform over {256^2, 512^2, 1280x720, 1920x1080}, mesh uniform
+    over the pool, 50/50 Blinn / NormalMap, shadow pass (2048^2) on half of them."""
+    rng = np.random.default_rng(seed)
+    res = ((256, 256), (512, 512), (1280, 720), (1920, 1080))
+    out = []
+    for _ in range(n):
+        m = int(rng.integers(len(pool)))
+        w, h = res[int(rng.integers(4))]
+        shader = BLINN if rng.random() < 0.5 else NORMALMAP
+        shadow = 2048 if rng.random() < 0.5 else 0
+        eye = orbit_eye(rng, pool[m].kind)
+        sd = U.shader_data(eye, w, h, enable_shadow=bool(shadow))
+        out.append(View(m, int(rng.integers(ntex)), shader, w, h, shadow, sd))
+    return out
+
+
+def serve_shadow_size(w: int, h: int) -> int:
+    """Square shadow map for a w x h request: the next power of two of the larger side,
+    clamped to [256, 2048]."""
+    s = 256
+    while s < max(w, h) and s < 2048:
+        s *= 2
+    return s
+
+
+@dataclasses.dataclass
+class Request(View):
+    arrival_ms: float = 0.0
+
+
+def request_stream(pool: list, n: int, rate_per_s: float, seed: int = 5, ntex: int = 4) -> list:
+    """Poisson arrivals at `rate_per_s`; mesh uniform from the pool; width and height
+    log-uniform over [128, 3840] x [128, 2160]; shader uniform over REQUEST_SHADERS; shadow
+    pass on half of the requests."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1000.0 / rate_per_s, n)
+    t = np.cumsum(gaps) - gaps[0]
+    out = []
+    for i in range(n):
+        m = int(rng.integers(len(pool)))
+        w = int(round(math.exp(rng.uniform(math.log(128), math.log(3840)))))
+        h = int(round(math.exp(rng.uniform(math.log(128), math.log(2160)))))
+        shader = int(REQUEST_SHADERS[int(rng.integers(len(REQUEST_SHADERS)))])
+        shadow = serve_shadow_size(w, h) if rng.random() < 0.5 else 0
+        eye = orbit_eye(rng, pool[m].kind)
+        sd = U.shader_data(eye, w, h, enable_shadow=bool(shadow))
+        out.append(Request(m, int(rng.integers(ntex)), shader, w, h, shadow, sd, float(t[i])))
+    return out
+
+
+def retime(requests: list, rate_per_s: float, seed: int = 9) -> list:
+    """The same requests with new Poisson arrival times."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1000.0 / rate_per_s, len(requests))
+    t = np.cumsum(gaps) - gaps[0]
+    return [dataclasses.replace(r, arrival_ms=float(ti)) for r, ti in zip(requests, t)]
+
+
+def view_frame(v: View, pool: list, textures: list) -> Frame:
+    """The Frame (oracle input) equal to a view / request."""
+    d, nm = textures[v.tex]
+    return Frame(pool[v.mesh].mesh, v.shader, v.sd, v.width, v.height, diffuse=d, normal=nm,
+                 shadow_size=(v.shadow, v.shadow), clear_rgba=(0, 0, 0, 255), shadow_clear_rgba=(0, 0, 0, 255),
+                 name=f"view_{pool[v.mesh].name}_{v.width}x{v.height}_{SHADER_NAMES[v.shader]}_sh{v.shadow}")
+
+
+def pool_textures(n: int = 4, size: int = 1024, seed: int = 17) -> list:
+    """n (diffuse RGBA8, tangent normal map RGB8) pairs of size^2."""
+    return [(noise_texture(size, size, 4, seed + 2 * i), normal_map_texture(size, size, seed + 2 * i + 1))
+            for i in range(n)]
+
+
 def prim_id_mesh(mesh: Mesh) -> Mesh:
     """Same v / vn / faces, one vt per face carrying the face id (lo 12 bits, hi bits)."""
     nf = mesh.nfaces

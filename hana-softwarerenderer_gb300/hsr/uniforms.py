@@ -180,6 +180,9 @@ def orthographic(right, top, near, far) -> Mat4:
     return m
 
 
+_IDENTITY_INV = None
+
+
 def shader_data(eye, width: int, height: int, *, target=(0, 0, 0), light=LIGHT_POS,
                 model: Mat4 | None = None, enable_shadow: bool = False,
                 material_color=WHITE, material_specular=WHITE, gloss=50.0, bump_scale=1.0,
@@ -189,18 +192,24 @@ def shader_data(eye, width: int, height: int, *, target=(0, 0, 0), light=LIGHT_P
     ``identity_mvp`` makes every matrix the identity (clip = (x, y, z, 1)), the setting of
     the depth-order stress workload.
     """
+    global _IDENTITY_INV
     eye, target, light = v3(eye), v3(target), v3(light)
     sd = np.zeros((), dtype=SHADER_DATA_DTYPE)
     aspect = F32(F32(width) / F32(height))
-    model = model or Mat4.identity()
     if identity_mvp:
         ident = Mat4.identity()
-        view = proj = lvp = cvp = ident
+        model = view = proj = lvp = cvp = ident
         model_I = ident
     else:
         view = lookat(eye, target, UP)
         proj = perspective(FOVY, aspect, NEAR, FAR)
-        model_I = model.invert()
+        if model is None:  # the identity's inverse (same routine, computed once)
+            model = Mat4.identity()
+            if _IDENTITY_INV is None:
+                _IDENTITY_INV = model.invert()
+            model_I = _IDENTITY_INV
+        else:
+            model_I = model.invert()
         lvp = orthographic(aspect, 1, 0, 5) @ lookat(light, target, UP)
         cvp = proj @ view
     sd["view_pos"] = eye

@@ -196,6 +196,72 @@ typedef struct hsr_stats {
 } hsr_stats;
 HSR_API int hsr_get_stats(hsr_stats* out);
 
+/* ---- plans: a batch recorded once into a CUDA graph and replayed ------------------------
+ * hsr_plan_create validates the draws (same rules as hsr_draw_batch), reserves the plan's own
+ * scratch, and records the whole launch sequence (descriptor upload, counter reset, seven
+ * kernels) into a CUDA graph.  Between replays only uniforms may change
+ * (hsr_plan_set_uniforms); meshes, textures, targets and shaders stay those of creation.
+ * hsr_plan_launch replays the graph on the library stream and returns at once;
+ * hsr_plan_wait blocks until it is done and re-runs it with larger scratch if the device
+ * reported an overflow (the targets are left untouched by an overflowing run). */
+typedef uint64_t hsr_plan;
+HSR_API int hsr_plan_create(const hsr_draw_desc* descs, int32_t n, hsr_plan* out);
+HSR_API int hsr_plan_set_uniforms(hsr_plan plan, int32_t draw, const hsr_shader_data* uniforms);
+HSR_API int hsr_plan_launch(hsr_plan plan);
+HSR_API int hsr_plan_wait(hsr_plan plan);
+HSR_API int hsr_plan_release(hsr_plan plan);
+
+/* ---- serving: continuous batching of render requests ------------------------------------
+ * A server owns a scheduler thread.  Requests (one DrawModel::draw each: an optional shadow
+ * pass into a shadow map of shadow_size^2, then the main pass) are queued by hsr_server_submit
+ * and admitted in arrival order while the framebuffer pool has room for their targets
+ * (pool_bytes, memory-based admission; a request larger than the whole pool fails with
+ * HSR_ERR_OUT_OF_MEMORY).  Whenever one of the `slots` in-flight batches is free, everything
+ * admitted so far (up to max_batch requests) becomes one launch sequence on that slot's
+ * stream, so batches overlap on the device.  Colour / depth / prim ids of each request are
+ * copied to the request's host pointers (page-locked memory recommended; NULL skips); the
+ * targets return to the pool.  Results equal those of the same request drawn alone. */
+typedef uint64_t hsr_server;
+typedef struct hsr_server_config {
+  uint64_t pool_bytes;     /* framebuffer pool budget for targets and shadow maps      */
+  int32_t max_batch;       /* requests per launch sequence                              */
+  int32_t slots;           /* launch sequences in flight (streams)                     */
+} hsr_server_config;
+
+typedef struct hsr_request {
+  hsr_mesh mesh;
+  int32_t shader;          /* hsr_shader_kind of the main pass                          */
+  hsr_texture diffuse;
+  hsr_texture normal;
+  int32_t width, height;   /* main target                                               */
+  int32_t shadow_size;     /* 0: no shadow pass; else an S x S shadow map (ShadowShader) */
+  hsr_shader_data uniforms;
+  uint8_t clear_rgba[4];
+  float clear_depth;
+  uint8_t shadow_clear_rgba[4];
+  float shadow_clear_depth;
+  uint8_t* out_rgba;       /* width*height*4 bytes, or NULL                            */
+  float* out_depth;        /* width*height floats, or NULL                             */
+  uint32_t* out_prim;      /* width*height, or NULL                                    */
+} hsr_request;
+
+typedef struct hsr_request_status {
+  int32_t status;          /* HSR_OK, HSR_ERR_BUSY while pending, or the failure        */
+  uint32_t batch;          /* sequence number of the batch that rendered it             */
+  uint32_t batch_requests; /* requests in that batch                                    */
+  uint32_t pad;
+  double submit_ms;        /* times on the server's clock (ms since creation)           */
+  double launch_ms;
+  double done_ms;
+} hsr_request_status;
+
+HSR_API int hsr_server_create(const hsr_server_config* cfg, hsr_server* out);
+HSR_API int hsr_server_submit(hsr_server s, const hsr_request* req, uint64_t* ticket);
+HSR_API int hsr_server_poll(hsr_server s, uint64_t ticket, hsr_request_status* out);   /* HSR_ERR_BUSY if pending */
+HSR_API int hsr_server_wait(hsr_server s, uint64_t ticket, int32_t timeout_ms, hsr_request_status* out);
+HSR_API int hsr_server_now_ms(hsr_server s, double* out);
+HSR_API int hsr_server_destroy(hsr_server s);   /* finishes in-flight work, fails queued requests */
+
 /* ---- timing of the last completed draw sequence (CUDA events on the library stream) --
  * batch_ms spans the upload of the view descriptors to the end of the raster kernel;
  * kernel_ms = {vertex, setup + post (clip / split), scan, scatter, raster}, filled when

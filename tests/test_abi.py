@@ -49,3 +49,40 @@ def test_no_device_means_error_not_fallback(libpath):
     assert b"device" in L.hsr_last_error() or len(L.hsr_last_error()) > 0
     h = ctypes.c_uint64()
     assert L.hsr_target_create(16, 16, ctypes.byref(h)) == hsr.ERR_NOT_INITIALIZED
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """The ctypes mirrors of the ABI structs have the C sizes and offsets."""
+    import shutil
+    import subprocess
+
+    if not shutil.which("gcc"):
+        pytest.skip("gcc not available")
+    import hsr
+
+    checks = {
+        "hsr_draw_desc": (hsr.DrawDesc, ["uniforms", "prim_base", "clear_rgba"]),
+        "hsr_request": (hsr.Request, ["uniforms", "clear_rgba", "shadow_clear_depth", "out_rgba", "out_prim"]),
+        "hsr_request_status": (hsr.RequestStatus, ["submit_ms", "done_ms"]),
+        "hsr_server_config": (hsr.ServerConfig, ["max_batch", "slots"]),
+        "hsr_timing": (hsr.Timing, ["launches", "h2d_bytes", "clipped_faces"]),
+        "hsr_stats": (hsr.Stats, ["kernel_launches"]),
+        "hsr_tuning": (hsr.Tuning, ["bin_factor"]),
+    }
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "hsr.h"', "int main(void) {"]
+    for cname, (_, fields) in checks.items():
+        lines.append(f'printf("%zu\\n", sizeof({cname}));')
+        for f in fields:
+            lines.append(f'printf("%zu\\n", offsetof({cname}, {f}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    exp = []
+    for _, (cls, fields) in checks.items():
+        exp.append(ctypes.sizeof(cls))
+        exp.extend(getattr(cls, f).offset for f in fields)
+    assert got == exp
+    assert ctypes.sizeof(hsr.Request) - hsr.Request.uniforms.offset >= hsr.SHADER_DATA_DTYPE.itemsize
