@@ -1,25 +1,38 @@
 """Benchmark of the GB300 draw path (one JSON line on rank 0).
 
-Workload (one step = one frame, the DrawModel::draw sequence: 2048^2 shadow pass, then the
-main pass): displaced icosphere subdivision 7 (327,680 triangles) + a 2-triangle ground
-plane submitted after it, 1024^2 RGBA8 diffuse + 1024^2 tangent-space normal map,
-1920x1080 FP32 depth + RGBA8 colour + prim ids, NormalMap + shadow shader; both clears
-are part of the frame.  Inputs are seeded synthetic data of those sizes.
+Headline workload — serving mixed render requests (each request is one DrawModel::draw,
+scene.h:53-99: an optional shadow pass, then the main pass):
+  16 resident meshes, 8,241,152 triangles in all (3x displaced icosphere-8, 6x icosphere-7,
+  4x 512^2 height-field grid, 3x icosphere-6), 4 texture pairs of 1024^2 (RGBA8 diffuse +
+  RGB8 tangent normal map); requests with mesh uniform over the pool, width / height
+  log-uniform over 128-3840 / 128-2160, shader uniform over ground / toon / texture /
+  texture-with-light / blinn / normal-map, a shadow pass on half of them (square map, next
+  power of two of the larger side, 256-2048); the colour of each request is read back.
+  Seeded synthetic data of those sizes (no public dataset is involved).
 
-value     frames/s with inputs resident in HBM: K frames, device time from CUDA events on
-          the library's stream around each frame, L2 flushed (512 MB write) between frames.
-e2e       frames/s through the public C ABI with host buffers: uniforms go host -> device
-          inside every frame and the frame's colour + depth come back into page-locked host
-          memory; wall-clock time.
-roofline  the kernel with the largest share of the frame: algorithmic bytes per launch /
-          its CUDA-event duration, against the measured HBM copy bandwidth.
-cpu_baseline  the oracle (C restatement of the reference) on the host cores, bounded sample.
+value     frames/s of the batched path with meshes and textures resident in HBM: each step
+          renders 64 requests of the stream as one launch sequence (the batch the server
+          forms); device time from CUDA events on the library's stream; L2 flushed (512 MB
+          write) before every step.
+e2e       frames/s through the public serving API (hsr_server_*) with host buffers: the
+          same requests submitted at once, uniforms host -> device and every colour
+          device -> page-locked host inside the timed region; wall clock.
+plain_per_frame   the same requests one at a time through the per-frame drop-in path
+          (targets created, both passes drawn, colour read back, targets released).
+serve     10,000 Poisson arrivals at two offered loads (80% of the plain path's capacity and
+          80% of the server's): frames/s and p50 / p99 latency from scheduled arrival, for
+          the server and for the plain path.
+roofline  the kernel with the largest share of the batched step: algorithmic bytes per
+          launch / its CUDA-event duration, against the measured HBM copy bandwidth.
+frame_1080p / batched_views_64   the single 1080p frame and the 64-view batched launch.
+cpu_baseline  the oracle (C restatement of the reference) on this host's cores, bounded
+          sample of the same request stream.
 
 --impl reference times the reference's CPU implementation of the path (the oracle port
 on a GPU host: the reference's Win32 sources do not build there) with every host thread.
 
-Multi-GPU (torchrun): each rank renders its own frames (replicas, no collective on the
-data path); value = all frames / slowest rank's time.
+Multi-GPU (torchrun): each rank serves its own requests (replicas, no collective on the data
+path); value = all frames / slowest rank's time.  The sub-results run on world size 1 only.
 """
 from __future__ import annotations
 
@@ -38,8 +51,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "hana-softwarerenderer_gb300"))
 
 METRIC = "frames/s + p50/p99 latency, batched serve vs plain per-frame; bit-exact depth"
-WORKLOAD = ("displaced icosphere-7 (327,680 tris) + 2-tri ground plane, 1920x1080, 2048^2 shadow map, "
-            "NormalMap + shadow, 1024^2 diffuse + normal map")
+SERVE_WORKLOAD = ("serving: 16 resident meshes (8,241,152 tris), 1024^2 diffuse + normal maps; requests with "
+                  "log-uniform 128-3840 x 128-2160 targets, 6 shaders, shadow pass on 50%, colour read back")
+FRAME_WORKLOAD = ("displaced icosphere-7 (327,680 tris) + 2-tri ground plane, 1920x1080, 2048^2 shadow map, "
+                  "NormalMap + shadow, 1024^2 diffuse + normal map")
+BATCH = 64          # requests per launch sequence (the server's max_batch)
+N_REQUESTS = 10000  # Poisson stream length
+SEED = 5
 
 
 def peaks() -> dict:
@@ -138,7 +156,7 @@ def dist_barrier(world: int):
 
 
 def kernel_bytes(t: dict) -> dict:
-    """Algorithmic bytes per launch of each kernel of one frame (both passes).
+    """Algorithmic bytes per launch of each kernel of one launch sequence.
 
     vertex : 12 B read + 16 B clip written per position, +16 B world position where the
              shader reads it; 12 B read + 16 B written per normal.
@@ -162,166 +180,337 @@ def kernel_bytes(t: dict) -> dict:
     }
 
 
-def ncu_traffic(kernel: str):
-    """DRAM bytes per launch of `kernel` from the committed ncu capture of this workload."""
+def ncu_traffic(workload: str, kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu capture of `workload`."""
     p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     if not os.path.exists(p):
         return None
     with open(p) as f:
-        return json.load(f)["dram_bytes_per_launch"].get(kernel)
+        d = json.load(f)
+    return d.get("workloads", {}).get(workload, {}).get("dram_bytes_per_launch", {}).get(kernel)
 
 
+def roofline(kernel_ms: dict, counts: dict, workload: str) -> dict:
+    mean_k = {k: statistics.mean(v) for k, v in kernel_ms.items()}
+    top = max(mean_k, key=mean_k.get)
+    kb = kernel_bytes(counts)
+    pk = peaks()
+    achieved = kb[top] / (mean_k[top] * 1e-3) / 1e9
+    return {"kernel": top, "bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"],
+            "peak_source": pk["source"], "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4),
+            "algorithmic_bytes": int(kb[top]), "ms": round(mean_k[top], 5), "traffic": ncu_traffic(workload, top),
+            "share": {k: round(v / sum(mean_k.values()), 4) for k, v in mean_k.items()}}
+
+
+def serve_inputs(n: int):
+    from hsr import scenes
+
+    pool = scenes.mesh_pool(scenes.SERVE_POOL_SPEC, seed=1)
+    tex = scenes.pool_textures(4, 1024, seed=17)
+    reqs = scenes.request_stream(pool, n, rate_per_s=1000.0, seed=SEED)
+    return pool, tex, reqs
+
+
+# ------------------------------------------------------------------------------------------
+# batched steps of the serving workload (value) + server / plain path (e2e, serve)
+# ------------------------------------------------------------------------------------------
 def run_ours(args, world, rank, local):
+    import torch
+
+    import hsr
+    from hsr import scenes
+    from hsr import serve as hserve
+
+    torch.cuda.set_device(local)
+    hsr.init(local)
+    t0 = time.time()
+    pool, tex, reqs = serve_inputs(N_REQUESTS)
+    rp = hserve.ResidentPool(pool, tex)
+    gen_s = time.time() - t0
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
+    # each rank serves its own slice of the stream
+    off = (rank * (args.warmup + args.steps) * BATCH) % len(reqs)
+    chunks = [[reqs[(off + i * BATCH + j) % len(reqs)] for j in range(BATCH)]
+              for i in range(args.warmup + args.steps)]
+
+    tuned = None
+    if args.tile:
+        hsr.set_tuning(tile=args.tile, warps_per_cta=4 if args.tile == 16 else 8)
+    elif not args.no_autotune:
+        vb = hserve.ViewBatch(rp, chunks[0])
+        tuned = hsr.autotune(vb.descs, reps=2)  # outside the timed region
+        vb.release()
+    hsr.set_profiling(True)
+
+    # ---- value: one launch sequence of 64 requests per step ------------------------------
+    step_ms, kernel_ms, launches, h2d, d2h = [], {k: [] for k in hsr.KERNELS}, 0, [], []
+    counts_sum: dict = {}
+    sampler = ClockSampler(local)
+    for i, chunk in enumerate(chunks):
+        timed = i >= args.warmup
+        vb = hserve.ViewBatch(rp, chunk)  # targets from the pool (untimed)
+        if timed and i == args.warmup:
+            dist_barrier(world)
+            torch.cuda.synchronize()
+            sampler.start()
+        flush.zero_()
+        torch.cuda.synchronize()
+        vb.draw_all()
+        t = hsr.last_timing()
+        vb.release()
+        if not timed:
+            continue
+        step_ms.append(t["batch_ms"])
+        for k, v in t["kernel_ms"].items():
+            kernel_ms[k].append(v)
+        launches += int(t["launches"])
+        h2d.append(int(t["h2d_bytes"]))
+        d2h.append(sum(r.width * r.height * 4 for r in chunk) + int(t["d2h_bytes"]))
+        for k in ("faces", "vertices", "normals", "records", "bin_pairs", "pixels", "shaded_pixels", "clipped_faces"):
+            counts_sum[k] = counts_sum.get(k, 0) + int(t[k])
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    dist_barrier(world)
+    frames = args.steps * BATCH
+    total_s = dist_max(sum(step_ms) / 1000.0, world)
+    value = world * frames / total_s
+    counts = {k: v / args.steps for k, v in counts_sum.items()}  # per step
+    roof = roofline(kernel_ms, counts, "serve_batch64")
+    hsr.set_profiling(False)
+
+    # ---- e2e: the same requests through hsr_server (all submitted at once) ----------------
+    timed_reqs = [r for c in chunks[args.warmup:] for r in c]
+    sat = scenes.retime(timed_reqs, 1e9)
+    hserve.serve_batched(rp, scenes.retime([r for c in chunks[:args.warmup] for r in c], 1e9), max_batch=BATCH)
+    dist_barrier(world)
+    e2e_run = hserve.serve_batched(rp, sat, max_batch=BATCH, slots=2)
+    e2e_s = dist_max(e2e_run["wall_s"], world)
+    e2e = {"value": round(world * frames / e2e_s, 2), "unit": "frames/s",
+           "h2d_bytes_per_step": int(statistics.mean(h2d)), "d2h_bytes_per_step": int(statistics.mean(d2h)),
+           "p50_ms": round(float(np.percentile(e2e_run["latency_ms"], 50)), 3),
+           "p99_ms": round(float(np.percentile(e2e_run["latency_ms"], 99)), 3),
+           "batches": e2e_run["batches"], "ok": e2e_run["ok"],
+           "note": "hsr_server, max_batch 64, 2 slots; all requests submitted at t=0; wall clock"}
+
+    out = {
+        "metric": METRIC, "value": round(value, 2), "unit": "frames/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(statistics.mean(step_ms), 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": SERVE_WORKLOAD, "frames_per_step": BATCH,
+                   "l2": "flushed (512 MB write) before every step; a step also writes ~1 GB of targets",
+                   "tuning": {k: getattr(hsr.get_tuning(), k) for k in ("tile", "warps_per_cta", "ctas_per_sm",
+                                                                      "bin_factor")},
+                   "autotuned": tuned is not None, "parallelism": f"replicas x{world}"},
+        "e2e": e2e,
+        "roofline": roof,
+        "kernel_ms": {k: round(statistics.mean(v), 4) for k, v in kernel_ms.items()},
+        "counts_per_step": {k: int(v) for k, v in counts.items()},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+
+    if world == 1 and not args.quick:
+        # ---- plain per-frame path on the same requests, then the Poisson streams ----------
+        hserve.serve_plain(rp, scenes.retime(chunks[0], 1e9))
+        plain_sat = hserve.serve_plain(rp, sat)
+        plain_fps = frames / plain_sat["wall_s"]
+        out["plain_per_frame"] = {
+            "frames_per_s": round(plain_fps, 2),
+            "p50_ms": round(float(np.percentile(plain_sat["latency_ms"], 50)), 3),
+            "p99_ms": round(float(np.percentile(plain_sat["latency_ms"], 99)), 3),
+            "batched_over_plain_e2e": round(e2e["value"] / plain_fps, 3),
+            "batched_over_plain_device": round(value / plain_fps, 3),
+            "note": "same requests, all at t=0, one at a time: hsr_target_create x2, hsr_draw_batch (shadow + "
+                    "main), hsr_target_download (colour), hsr_target_release x2; wall clock"}
+        out["serve"] = serve_poisson(rp, reqs, plain_fps, e2e["value"], args)
+        out["frame_1080p"] = run_frame(args)
+        out["batched_views_64"] = run_views(args)
+    rp.release()
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(pool, tex, reqs, args.cpu_seconds)
+    out["gen_s"] = round(gen_s, 2)
+    return out
+
+
+def serve_poisson(rp, reqs, plain_fps: float, server_fps: float, args) -> dict:
+    """The 10,000-request Poisson stream at two offered loads, server vs plain path."""
+    from hsr import scenes
+    from hsr import serve as hserve
+
+    res = {"requests": len(reqs), "arrivals": "Poisson"}
+    for name, rate in (("load_plain80", 0.8 * plain_fps), ("load_server80", 0.8 * server_fps)):
+        stream = scenes.retime(reqs, rate, seed=11)
+        b = hserve.serve_batched(rp, stream, max_batch=BATCH, slots=2)
+        p = hserve.serve_plain(rp, stream)
+        sb = hserve.latency_summary(b, len(stream))
+        sp = hserve.latency_summary(p, len(stream))
+        res[name] = {"rate_per_s": round(rate, 1),
+                     "server": {k: round(v, 3) for k, v in sb.items()} | {"mean_batch": round(b["mean_batch"], 2),
+                                                                         "ok": b["ok"]},
+                     "plain": {k: round(v, 3) for k, v in sp.items()}}
+    return res
+
+
+def run_frame(args) -> dict:
+    """The single 1080p frame with its 2048^2 shadow pass (device time + plain calls)."""
     import torch
 
     import hsr
     from hsr import frame as hframe
     from hsr import scenes
 
-    torch.cuda.set_device(local)
-    hsr.init(local)
-    t0 = time.time()
     fr = scenes.displaced_frame()
-    gen_s = time.time() - t0
     g = hframe.GpuFrame(fr)
-    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
-
-    tuned = None
-    if args.tile:
-        hsr.set_tuning(tile=args.tile, warps_per_cta=4 if args.tile == 16 else 8)
-    elif not args.no_autotune:
-        tuned = hsr.autotune(g.descs, reps=3)  # outside the timed region
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    old = hsr.get_tuning()
+    hsr.autotune(g.descs, reps=3)
     hsr.set_profiling(True)
-    for _ in range(args.warmup):
+    for _ in range(3):
         g.render()
-    # ---- timed region (device) ----------------------------------------------------------
-    sampler = ClockSampler(local)
-    dist_barrier(world)
-    torch.cuda.synchronize()
-    sampler.start()
-    frame_ms, kernel_ms, timings = [], {k: [] for k in hsr.KERNELS}, None
+    ms, kms, t = [], {k: [] for k in hsr.KERNELS}, None
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         g.render()
-        timings = hsr.last_timing()
-        frame_ms.append(timings["batch_ms"])
-        for k, v in timings["kernel_ms"].items():
-            kernel_ms[k].append(v)
-    torch.cuda.synchronize()
-    clocks = sampler.stop()
-    dist_barrier(world)
-    total_s = sum(frame_ms) / 1000.0
-    total_s_max = dist_max(total_s, world)
-    value = world * args.steps / total_s_max
-
-    # ---- plain per-frame path: one hsr_draw per pass (two synchronous calls) ------------
-    plain_ms = []
+        t = hsr.last_timing()
+        ms.append(t["batch_ms"])
+        for k, v in t["kernel_ms"].items():
+            kms[k].append(v)
+    plain = []
     for _ in range(max(3, args.steps // 2)):
         flush.zero_()
         torch.cuda.synchronize()
         s0 = time.perf_counter()
         g.render(batched=False)
-        plain_ms.append((time.perf_counter() - s0) * 1000.0)
-
-    # ---- end to end through the C ABI with host buffers ---------------------------------
+        plain.append((time.perf_counter() - s0) * 1000.0)
     hsr.set_profiling(False)
-    pc = hsr.PinnedArray((fr.height, fr.width, 4), np.uint8)
-    pd = hsr.PinnedArray((fr.height, fr.width), np.float32)
-    e2e_ms = []
-    for i in range(args.warmup + args.steps):
-        flush.zero_()
+    counts = {k: int(t[k]) for k in ("faces", "vertices", "normals", "records", "bin_pairs", "pixels",
+                                     "shaded_pixels", "clipped_faces")}
+    res = {"workload": FRAME_WORKLOAD, "frames_per_s": round(1000.0 / statistics.mean(ms), 2),
+           "ms_p50": round(float(np.percentile(ms, 50)), 4), "ms_p99": round(float(np.percentile(ms, 99)), 4),
+           "plain_two_draw_calls_frames_per_s": round(1000.0 / statistics.mean(plain), 2),
+           "kernel_ms": {k: round(statistics.mean(v), 4) for k, v in kms.items()},
+           "roofline": roofline(kms, counts, "frame_1080p"), "counts": counts,
+           "tuning": {k: getattr(hsr.get_tuning(), k) for k in ("tile", "warps_per_cta", "ctas_per_sm")}}
+    g.release()
+    hsr.set_tuning(tile=old.tile, warps_per_cta=old.warps_per_cta, ctas_per_sm=old.ctas_per_sm)
+    return res
+
+
+def run_views(args) -> dict:
+    """64 views in one launch sequence: replayed CUDA graph vs one hsr_draw_batch vs one view
+    at a time (8 meshes of 2,048-1,310,720 triangles, 256^2-1920x1080, Blinn / NormalMap,
+    2048^2 shadow pass on half of them)."""
+    import torch
+
+    import hsr
+    from hsr import scenes
+    from hsr import serve as hserve
+
+    pool = scenes.mesh_pool(scenes.VIEW_POOL_SPEC, seed=1)
+    tex = scenes.pool_textures(4, 1024, seed=17)
+    rp = hserve.ResidentPool(pool, tex)
+    views = scenes.view_set(pool, 64, seed=3)
+    vb = hserve.ViewBatch(rp, views)
+    old = hsr.get_tuning()
+    tuned = hsr.autotune(vb.descs, reps=2)
+    plan = vb.plan()
+
+    def timed(fn, k):
         torch.cuda.synchronize()
         s0 = time.perf_counter()
-        g.render()
-        g.main.download(color=True, depth=True, prim=False, out={"color": pc.array, "depth": pd.array})
-        if i >= args.warmup:
-            e2e_ms.append((time.perf_counter() - s0) * 1000.0)
-    e2e_t = hsr.last_timing()
-    h2d = int(e2e_t["h2d_bytes"])
-    d2h = int(pc.array.nbytes + pd.array.nbytes + e2e_t["d2h_bytes"])
-    e2e_s = dist_max(sum(e2e_ms) / 1000.0, world)
-    pc.release()
-    pd.release()
+        for _ in range(k):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - s0) / k
 
-    # ---- roofline of the dominant kernel ------------------------------------------------
-    mean_k = {k: statistics.mean(v) for k, v in kernel_ms.items()}
-    top = max(mean_k, key=mean_k.get)
-    kb = kernel_bytes(timings)
-    pk = peaks()
-    achieved = kb[top] / (mean_k[top] * 1e-3) / 1e9
-    roof = {"kernel": top, "bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"],
-            "peak_source": pk["source"], "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4),
-            "algorithmic_bytes": int(kb[top]), "ms": round(mean_k[top], 5),
-            "traffic": args.traffic_bytes if args.traffic_bytes else ncu_traffic(top),
-            "share": {k: round(v / sum(mean_k.values()), 4) for k, v in mean_k.items()}}
+    def replay():
+        plan.launch()
+        plan.wait()
 
-    out = {
-        "metric": METRIC, "value": round(value, 2), "unit": "frames/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(statistics.mean(frame_ms), 5),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "frames_per_step": 1, "l2": "flushed (512 MB write) between timed frames",
-                   "tuning": {k: getattr(hsr.get_tuning(), k) for k in ("tile", "warps_per_cta", "ctas_per_sm",
-                                                                      "bin_factor")},
-                   "autotuned": tuned is not None, "parallelism": f"replicas x{world}"},
-        "latency_ms": {"p50": round(float(np.percentile(frame_ms, 50)), 5),
-                       "p99": round(float(np.percentile(frame_ms, 99)), 5)},
-        "plain_per_frame": {"ms_p50": round(float(np.percentile(plain_ms, 50)), 4),
-                            "frames_per_s": round(1000.0 / statistics.mean(plain_ms), 2),
-                            "note": "two synchronous hsr_draw calls per frame, wall clock"},
-        "e2e": {"value": round(world * args.steps / e2e_s, 2), "unit": "frames/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "p50_ms": round(float(np.percentile(e2e_ms, 50)), 4)},
-        "roofline": roof,
-        "kernel_ms": {k: round(v, 5) for k, v in mean_k.items()},
-        "counts": {k: int(timings[k]) for k in ("faces", "vertices", "records", "bin_pairs", "pixels",
-                                                  "shaded_pixels", "clipped_faces")},
-        "gpu_launches": int(timings["launches"]) * args.steps,
-        "clocks": clocks,
-    }
-    g.release()
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(fr, args.cpu_seconds)
-    out["gen_s"] = round(gen_s, 2)
-    return out
+    for fn in (vb.draw_each, vb.draw_all, replay):
+        for _ in range(3):
+            fn()
+    k = max(5, args.steps // 3)
+    te, ta, tp = timed(vb.draw_each, k), timed(vb.draw_all, k), timed(replay, k)
+    res = {"views": 64, "pixels_per_batch": vb.pixels(),
+           "triangles_in_pool": int(sum(p.mesh.nfaces for p in pool)),
+           "graph_replay_frames_per_s": round(64 / tp, 1), "draw_batch_frames_per_s": round(64 / ta, 1),
+           "per_view_frames_per_s": round(64 / te, 1), "graph_over_per_view": round(te / tp, 3),
+           "tuning": tuned, "note": "wall clock per batch; per view = one hsr_draw_batch (shadow + main) per view"}
+    plan.release()
+    vb.release()
+    rp.release()
+    hsr.set_tuning(tile=old.tile, warps_per_cta=old.warps_per_cta, ctas_per_sm=old.ctas_per_sm)
+    return res
 
 
-def cpu_baseline(fr, seconds: float, threads: int | None = None) -> dict:
-    """The oracle (C restatement, 1 frame per thread per round) on this host's cores."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
-
-    threads = threads or os.cpu_count() or 1
-    one = oracle.bench_frames(fr, 1, 1)
-    rounds = max(1, int(round(seconds / max(one, 1e-3))))
-    s = oracle.bench_frames(fr, rounds, threads)
-    frames = rounds * threads
-    return {"value": round(frames / s, 4), "unit": "frames/s", "cores": threads, "kind": "port",
-            "sample": f"{frames} frames of the benchmark workload ({rounds} per thread), {s:.1f} s wall; "
-                      f"1 frame on 1 core = {one * 1000:.0f} ms"}
-
-
-def run_reference(args, world, rank):
-    """The reference's CPU implementation of the path with every host thread."""
-    if rank != 0:
-        return None
+# ------------------------------------------------------------------------------------------
+# CPU: the oracle on a bounded sample of the same request stream
+# ------------------------------------------------------------------------------------------
+def cpu_render_requests(pool, tex, reqs, threads: int, seconds: float | None = None) -> tuple:
+    """`threads` threads render `reqs` in order, one request per task; with `seconds`, no
+    task starts after that much wall time.  Returns (requests rendered, wall seconds)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     from hsr import scenes
 
-    fr = scenes.displaced_frame()
+    lock = threading.Lock()
+    nxt = [0]
+    done = [0]
+    s0 = time.perf_counter()
+
+    def worker():
+        while True:
+            with lock:
+                i = nxt[0]
+                if i >= len(reqs) or (seconds is not None and time.perf_counter() - s0 >= seconds):
+                    return
+                nxt[0] += 1
+            oracle.render_frame(scenes.view_frame(reqs[i], pool, tex))
+            with lock:
+                done[0] += 1
+
+    ths = [threading.Thread(target=worker) for _ in range(threads)]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    return done[0], time.perf_counter() - s0
+
+
+def cpu_baseline(pool, tex, reqs, seconds: float, threads: int | None = None) -> dict:
+    threads = threads or os.cpu_count() or 1
+    n, s = cpu_render_requests(pool, tex, reqs, threads, seconds)
+    return {"value": round(n / s, 4), "unit": "frames/s", "cores": threads, "kind": "port",
+            "sample": f"the first {n} requests of the serving stream, {threads} threads, {s:.1f} s wall "
+                      f"(no request starts after {seconds:.0f} s)"}
+
+
+def run_reference(args, world, rank):
+    """The reference's CPU implementation of the path with every host thread, on the same
+    request stream: each step renders the next 64 requests (one step of ours), the threads
+    taking requests as they free up."""
+    if rank != 0:
+        return None
+    pool, tex, reqs = serve_inputs(N_REQUESTS)
     threads = os.cpu_count() or 1
-    for _ in range(args.warmup):
-        oracle.bench_frames(fr, 1, threads)
-    secs = [oracle.bench_frames(fr, 1, threads) for _ in range(args.steps)]
-    value = args.steps * threads / sum(secs)
+    pos = 0
+    secs = []
+    for i in range(args.warmup + args.steps):
+        n, s = cpu_render_requests(pool, tex, reqs[pos:pos + BATCH], threads)
+        pos = (pos + BATCH) % (len(reqs) - BATCH)
+        if i >= args.warmup:
+            secs.append(s)
+    value = args.steps * BATCH / sum(secs)
     per = [s * 1000.0 for s in secs]
     return {
         "metric": METRIC, "value": round(value, 4), "unit": "frames/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(statistics.mean(per), 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-        "config": {"workload": WORKLOAD, "frames_per_step": threads, "l2": "n/a (host)"},
+        "config": {"workload": SERVE_WORKLOAD, "frames_per_step": BATCH, "l2": "n/a (host)"},
         "cpu_baseline": {"value": round(value, 4), "unit": "frames/s", "cores": threads, "kind": "port",
-                         "sample": f"{threads} frames per step ({threads} threads x 1 frame), {args.steps} steps"},
+                         "sample": f"{BATCH} distinct requests per step on {threads} threads, {args.steps} steps"},
         "e2e": {"value": round(value, 4), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gpu_launches": 0,
     }
@@ -335,10 +524,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--quick", action="store_true", help="headline only (no plain / Poisson / sub-workloads)")
     ap.add_argument("--tile", type=int, default=0, help="fix the raster tile (8 or 16) instead of autotuning")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--traffic-bytes", type=float, default=0.0,
-                    help="DRAM bytes of the dominant kernel per launch from an ncu capture")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()

@@ -415,10 +415,10 @@ def request_stream(pool: list, n: int, rate_per_s: float, seed: int = 5, ntex: i
     log-uniform over [128, 3840] x [128, 2160]; shader uniform over REQUEST_SHADERS; shadow
     pass on half of the requests."""
     rng = np.random.default_rng(seed)
-    gaps = rng.exponential(1000.0 / rate_per_s, n)
+    gaps = np.random.default_rng(seed + 7919).exponential(1000.0 / rate_per_s, n)
     t = np.cumsum(gaps) - gaps[0]
     out = []
-    for i in range(n):
+    for i in range(n):  # request i does not depend on n or on the rate
         m = int(rng.integers(len(pool)))
         w = int(round(math.exp(rng.uniform(math.log(128), math.log(3840)))))
         h = int(round(math.exp(rng.uniform(math.log(128), math.log(2160)))))
