@@ -112,6 +112,36 @@ __device__ __forceinline__ F3 tex_normal(const DView& v, float u, float t, const
   return r;
 }
 
+// barycentric() at the integer pixel (px, py) and the inside test of rasterize_triangle
+// (graphics.cpp:222-233, :352-357) for a triangle with screen corner A = (ax, ay), edges
+// e1 = B - A, e2 = C - A and u.z = e2.x*e1.y - e1.x*e2.y (|u.z| > 0.01).  Weights are
+// (1 - (u.x+u.y)/u.z, u.y/u.z, u.x/u.z); the pixel is covered when all three are >= 0.
+// `exact` selects the literal divisions; otherwise the sign test on u.x, u.y, u.x+u.y
+// against u.z decides coverage without dividing (equal to the divisions' verdict for
+// coordinates in the range setup checks) and the weights are computed only when covered.
+// The raster and the setup-side cull of pixel-less triangles share this function, so both
+// take the same decision for every pixel.
+__device__ __forceinline__ bool cover_test(float ax, float ay, float e1x, float e1y, float e2x, float e2y, float uz,
+                                           bool exact, float pxf, float pyf, float& b0, float& b1, float& b2) {
+  const float dx = fs(ax, pxf), dy = fs(ay, pyf);
+  const float ux = fs(fm(e1x, dy), fm(dx, e1y));
+  const float uy = fs(fm(dx, e2y), fm(e2x, dy));
+  const float su = fa(ux, uy);
+  if (!exact) {
+    const bool covered = (uz < 0.f) ? (su >= uz && uy <= 0.f && ux <= 0.f) : (su <= uz && uy >= 0.f && ux >= 0.f);
+    if (covered) {
+      b0 = fs(1.f, fd(su, uz));
+      b1 = fd(uy, uz);
+      b2 = fd(ux, uz);
+    }
+    return covered;
+  }
+  b0 = fs(1.f, fd(su, uz));
+  b1 = fd(uy, uz);
+  b2 = fd(ux, uz);
+  return !(b0 < 0.f || b1 < 0.f || b2 < 0.f);
+}
+
 // viewport_transform (maths.cpp:20-25)
 __device__ __forceinline__ F3 viewport(int32_t w, int32_t h, F3 ndc) {
   return {fm(fm(fa(ndc.x, 1.f), 0.5f), (float)w), fm(fm(fa(ndc.y, 1.f), 0.5f), (float)h), fm(fa(ndc.z, 1.f), 0.5f)};

@@ -71,6 +71,8 @@ int launch_vertex(const DView* views, const Chunk* chunks, int nchunks, cudaStre
 // ---------------------------------------------------------------------------------------
 // setup stage
 // ---------------------------------------------------------------------------------------
+constexpr int kSetupCoverPixels = 8;  // pixel ranges up to this size are tested in setup
+
 __device__ __forceinline__ bool coord_ok(float c) {
   float a = fabsf(c);
   return (a == 0.f) || (a >= 0x1p-8f && a <= 0x1p20f);
@@ -111,14 +113,25 @@ __device__ __forceinline__ bool build_rec(const DView& v, float4 c0, float4 c1, 
   const float e2x = fs(s2.x, s0.x), e2y = fs(s2.y, s0.y);
   const float uz = fs(fm(e2x, e1y), fm(e1x, e2y));
   if (!(fabsf(uz) > 0.01f)) return false;  // degenerate: every pixel gets (-1,1,1)
+  const bool ok = coord_ok(s0.x) && coord_ok(s0.y) && coord_ok(s1.x) && coord_ok(s1.y) &&
+                  coord_ok(s2.x) && coord_ok(s2.y) && fabsf(uz) <= 0x1p30f;
+  // a small pixel range is tested here with the raster's own coverage test: a triangle
+  // that covers none of its pixels would only be visited and rejected pixel by pixel
+  if ((x1 - x0 + 1) * (y1 - y0 + 1) <= kSetupCoverPixels) {
+    bool any = false;
+    for (int32_t y = y0; y <= y1 && !any; y++)
+      for (int32_t x = x0; x <= x1 && !any; x++) {
+        float b0, b1, b2;
+        any = cover_test(s0.x, s0.y, e1x, e1y, e2x, e2y, uz, !ok, (float)x, (float)y, b0, b1, b2);
+      }
+    if (!any) return false;
+  }
   r.ax = s0.x; r.ay = s0.y; r.e1x = e1x; r.e1y = e1y;
   r.e2x = e2x; r.e2y = e2y; r.uz = uz; r.d0 = s0.z;
   r.d1 = s1.z; r.d2 = s2.z;
   r.seq = seq;
   r.xr = (uint32_t)x0 | ((uint32_t)x1 << 16);
   r.yr = (uint32_t)y0 | ((uint32_t)y1 << 16);
-  const bool ok = coord_ok(s0.x) && coord_ok(s0.y) && coord_ok(s1.x) && coord_ok(s1.y) &&
-                  coord_ok(s2.x) && coord_ok(s2.y) && fabsf(uz) <= 0x1p30f;
   r.view = view | ((ok ? 0u : kRecExact) << kRecFlagShift);
   r.rsv = 0u;
   r.pad = 0u;
@@ -272,7 +285,7 @@ __device__ __forceinline__ uint32_t warp_append(bool want, uint32_t* counter) {
   return want ? base + (uint32_t)__popc(m & ((1u << lane) - 1u)) : ~0u;
 }
 
-__global__ void __launch_bounds__(kSetupThreads) k_setup(const DView* __restrict__ views,
+__global__ void __launch_bounds__(kSetupThreads, 4) k_setup(const DView* __restrict__ views,
                                                          const Chunk* __restrict__ chunks, int T, Scratch sc) {
   const Chunk ch = chunks[blockIdx.x];
   const DView& v = views[ch.view];

@@ -251,25 +251,8 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
             const int ly = (int)((box >> 8) & 255u) + (int)qy;
             p = ly * T + lx;
             const RasterRec& r = srec[warp][j];
-            const float pxf = (float)(ox + lx), pyf = (float)(oy + ly);
-            // barycentric() at integer P (graphics.cpp:222-233)
-            const float dx = fs(r.ax, pxf), dy = fs(r.ay, pyf);
-            const float ux = fs(fm(r.e1x, dy), fm(dx, r.e1y));
-            const float uy = fs(fm(dx, r.e2y), fm(r.e2x, dy));
-            const float su = fa(ux, uy);
-            if (!((r.view >> kRecFlagShift) & kRecExact)) {
-              covered = (r.uz < 0.f) ? (su >= r.uz && uy <= 0.f && ux <= 0.f) : (su <= r.uz && uy >= 0.f && ux >= 0.f);
-              if (covered) {
-                b0 = fs(1.f, fd(su, r.uz));
-                b1 = fd(uy, r.uz);
-                b2 = fd(ux, r.uz);
-              }
-            } else {
-              b0 = fs(1.f, fd(su, r.uz));
-              b1 = fd(uy, r.uz);
-              b2 = fd(ux, r.uz);
-              covered = !(b0 < 0.f || b1 < 0.f || b2 < 0.f);
-            }
+            covered = cover_test(r.ax, r.ay, r.e1x, r.e1y, r.e2x, r.e2y, r.uz, ((r.view >> kRecFlagShift) & kRecExact) != 0u,
+                                 (float)(ox + lx), (float)(oy + ly), b0, b1, b2);
             if (covered) {
               // interpolate_depth (graphics.cpp:186-194)
               const float z = fa(fa(fa(0.f, fm(r.d2, b2)), fm(r.d1, b1)), fm(r.d0, b0));
