@@ -235,7 +235,8 @@ def run_ours(args, world, rank, local):
 
     tuned = None
     if args.tile:
-        hsr.set_tuning(tile=args.tile, warps_per_cta=4 if args.tile == 16 else 8)
+        hsr.set_tuning(tile=args.tile, warps_per_cta=args.warps or (4 if args.tile == 16 else 8),
+                       ctas_per_sm=args.ctas or None)
     elif not args.no_autotune:
         vb = hserve.ViewBatch(rp, chunks[0])
         tuned = hsr.autotune(vb.descs, reps=2)  # outside the timed region
@@ -526,6 +527,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--quick", action="store_true", help="headline only (no plain / Poisson / sub-workloads)")
     ap.add_argument("--tile", type=int, default=0, help="fix the raster tile (8 or 16) instead of autotuning")
+    ap.add_argument("--warps", type=int, default=0, help="with --tile: warps per CTA of the raster (4 or 8)")
+    ap.add_argument("--ctas", type=int, default=0, help="with --tile: raster CTAs per SM")
     ap.add_argument("--no-autotune", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

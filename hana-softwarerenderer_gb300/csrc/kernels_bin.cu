@@ -119,6 +119,7 @@ __global__ void __launch_bounds__(256) k_scatter(const DView* __restrict__ views
   const uint32_t nrec = min(sc.ctl->rec_count, sc.rec_cap);
   if (sc.ctl->error & (kErrBinOverflow | kErrRecOverflow | kErrClipOverflow | kErrScanTimeout)) return;
   const uint32_t stride = gridDim.x * blockDim.x;
+  const int ts = __ffs(T) - 1;  // T is a power of two
   // warp-uniform trip count so every lane takes part in the warp-level collectives
   for (uint32_t i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < nrec; i0 += stride) {
     const uint32_t i = i0 + (uint32_t)lane;
@@ -130,15 +131,17 @@ __global__ void __launch_bounds__(256) k_scatter(const DView* __restrict__ views
       const DView& v = views[r.view & kRecViewMask];
       tbase = v.tile_base;
       tiles_x = v.tiles_x;
-      tx0 = (int)(xr & 0xffffu) / T;
-      ty0 = (int)(yr & 0xffffu) / T;
-      ntw = (int)(xr >> 16) / T - tx0 + 1;
-      nt = ntw * ((int)(yr >> 16) / T - ty0 + 1);
+      tx0 = (int)(xr & 0xffffu) >> ts;
+      ty0 = (int)(yr & 0xffffu) >> ts;
+      ntw = ((int)(xr >> 16) >> ts) - tx0 + 1;
+      nt = ntw * (((int)(yr >> 16) >> ts) - ty0 + 1);
     }
     const int my_n = min(nt, kMaxRecordTiles);
     const int maxn = __reduce_max_sync(kFull, my_n);
+    int kx = 0, ky = 0;  // tile k of the rectangle, row-major
     for (int k = 0; k < maxn; k++) {
-      const int tile = (k < my_n) ? tbase + (ty0 + k / ntw) * tiles_x + tx0 + k % ntw : -1;
+      const int tile = (k < my_n) ? tbase + (ty0 + ky) * tiles_x + tx0 + kx : -1;
+      if (++kx == ntw) { kx = 0; ky++; }
       const unsigned grp = __match_any_sync(kFull, tile);
       const int leader = __ffs(grp) - 1;
       uint32_t b = 0;

@@ -183,28 +183,35 @@ __device__ __forceinline__ void store_payload(Payload* dst, const Payload& p, in
     if (q < nf4) d[q] = s[q];
 }
 
+// Tile rectangle of a record; T is a power of two (8 or 16).
 __device__ __forceinline__ void rec_tiles(const RasterRec& r, int T, int& tx0, int& ty0, int& ntw, int& nt) {
+  const int ts = __ffs(T) - 1;
   const int x0 = (int)(r.xr & 0xffffu), x1 = (int)(r.xr >> 16);
   const int y0 = (int)(r.yr & 0xffffu), y1 = (int)(r.yr >> 16);
-  tx0 = x0 / T;
-  ty0 = y0 / T;
-  ntw = x1 / T - tx0 + 1;
-  nt = ntw * (y1 / T - ty0 + 1);
+  tx0 = x0 >> ts;
+  ty0 = y0 >> ts;
+  ntw = (x1 >> ts) - tx0 + 1;
+  nt = ntw * ((y1 >> ts) - ty0 + 1);
 }
 
-// Append the records of a warp (at most one per lane, each touching <= kMaxRecordTiles
-// tiles) and count the tiles they touch, aggregating equal tiles across lanes.  All 32
-// lanes call this.
-__device__ void append_small(bool valid, const RasterRec& r, const Payload& pl, int nf4, const DView& v, int T,
-                             const Scratch& sc) {
+// Slot of this lane's item when `want`, one atomicAdd per warp (~0u otherwise).
+__device__ __forceinline__ uint32_t warp_reserve(bool want, uint32_t* counter) {
   const int lane = threadIdx.x & 31;
-  const unsigned m = __ballot_sync(kFull, valid);
-  if (!m) return;
+  const unsigned m = __ballot_sync(kFull, want);
+  if (!m) return ~0u;
   const int leader = __ffs(m) - 1;
   uint32_t base = 0;
-  if (lane == leader) base = atomicAdd(&sc.ctl->rec_count, (uint32_t)__popc(m));
+  if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
   base = __shfl_sync(kFull, base, leader);
-  const uint32_t slot = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+  return want ? base + (uint32_t)__popc(m & ((1u << lane) - 1u)) : ~0u;
+}
+
+// Store the records of a warp at their reserved slots (at most one per lane, each touching
+// <= kMaxRecordTiles tiles) and count the tiles they touch, aggregating equal tiles across
+// lanes.  All 32 lanes call this.
+__device__ void append_small(bool valid, uint32_t slot, const RasterRec& r, const Payload& pl, int nf4, const DView& v,
+                             int T, const Scratch& sc) {
+  const int lane = threadIdx.x & 31;
   const bool ok = valid && slot < sc.rec_cap;
   if (valid && !ok) atomicOr(&sc.ctl->error, kErrRecOverflow);
   int tx0 = 0, ty0 = 0, ntw = 1, nt = 0;
@@ -216,10 +223,12 @@ __device__ void append_small(bool valid, const RasterRec& r, const Payload& pl, 
     rec_tiles(r, T, tx0, ty0, ntw, nt);
   }
   const int maxn = __reduce_max_sync(kFull, nt);
+  int kx = 0, ky = 0;  // tile k of the rectangle = (kx, ky), row-major
   for (int k = 0; k < maxn; k++) {
-    const int tile = (k < nt) ? v.tile_base + (ty0 + k / ntw) * v.tiles_x + tx0 + k % ntw : -1;
+    const int tile = (k < nt) ? v.tile_base + (ty0 + ky) * v.tiles_x + tx0 + kx : -1;
     const unsigned grp = __match_any_sync(kFull, tile);
     if (tile >= 0 && lane == __ffs(grp) - 1) atomicAdd(&sc.tile_count[tile], (uint32_t)__popc(grp));
+    if (++kx == ntw) { kx = 0; ky++; }
   }
 }
 
@@ -273,17 +282,6 @@ __device__ __forceinline__ bool clip_trivially_empty(float4 c0, float4 c1, float
 constexpr int kSetupThreads = 256;
 constexpr int kPolyStride = kVaryings;  // floats per polygon vertex in shared memory
 
-// Warp-aggregated append of one item per participating lane; returns the slot or ~0u.
-__device__ __forceinline__ uint32_t warp_append(bool want, uint32_t* counter) {
-  const int lane = threadIdx.x & 31;
-  const unsigned m = __ballot_sync(kFull, want);
-  if (!m) return ~0u;
-  const int leader = __ffs(m) - 1;
-  uint32_t base = 0;
-  if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
-  base = __shfl_sync(kFull, base, leader);
-  return want ? base + (uint32_t)__popc(m & ((1u << lane) - 1u)) : ~0u;
-}
 
 __global__ void __launch_bounds__(kSetupThreads, 4) k_setup(const DView* __restrict__ views,
                                                          const Chunk* __restrict__ chunks, int T, Scratch sc) {
@@ -329,11 +327,12 @@ __global__ void __launch_bounds__(kSetupThreads, 4) k_setup(const DView* __restr
   int tx0, ty0, ntw, nt = 0;
   if (valid) rec_tiles(r, T, tx0, ty0, ntw, nt);
   const bool big = valid && nt > kMaxRecordTiles;
-  append_small(valid && !big, r, pl, payload_f4(v.shader), v, T, sc);
+  const uint32_t slot = warp_reserve(valid && !big, &sc.ctl->rec_count);
+  append_small(valid && !big, slot, r, pl, payload_f4(v.shader), v, T, sc);
 
   // huge triangles and faces that need the clipper are queued for k_post, which spreads
   // them over the whole GPU instead of leaving one warp to work through a cluster of them
-  const uint32_t bslot = warp_append(big, &sc.ctl->big_count);
+  const uint32_t bslot = warp_reserve(big, &sc.ctl->big_count);
   if (big) {
     if (bslot < sc.big_cap) {
       store_rec(&sc.bigq[bslot].rec, r);
@@ -342,7 +341,7 @@ __global__ void __launch_bounds__(kSetupThreads, 4) k_setup(const DView* __restr
       atomicOr(&sc.ctl->error, kErrBigOverflow);
     }
   }
-  const uint32_t cslot = warp_append(needs_clip, &sc.ctl->clip_count);
+  const uint32_t cslot = warp_reserve(needs_clip, &sc.ctl->clip_count);
   if (needs_clip) {
     if (cslot < sc.clip_cap) sc.clipq[cslot] = make_int2(ch.view, f);
     else atomicOr(&sc.ctl->error, kErrClipOverflow);
@@ -409,8 +408,9 @@ __device__ void clip_face(const DView& v, int view, int face, int T, const Scrat
   if (valid) rec_tiles(r, T, tx0, ty0, ntw, nt);
   const bool big = valid && nt > kMaxRecordTiles;
   const int nf4 = payload_f4(v.shader);
-  append_small(valid && !big, r, pl, nf4, v, T, sc);
-  const uint32_t bslot = warp_append(big, &sc.ctl->big_count);
+  const uint32_t slot = warp_reserve(valid && !big, &sc.ctl->rec_count);
+  append_small(valid && !big, slot, r, pl, nf4, v, T, sc);
+  const uint32_t bslot = warp_reserve(big, &sc.ctl->big_count);
   if (big) {
     if (bslot < sc.big_cap) {
       store_rec(&sc.bigq[bslot].rec, r);
