@@ -55,6 +55,8 @@ SERVE_WORKLOAD = ("serving: 16 resident meshes (8,241,152 tris), 1024^2 diffuse 
                   "log-uniform 128-3840 x 128-2160 targets, 6 shaders, shadow pass on 50%, colour read back")
 FRAME_WORKLOAD = ("displaced icosphere-7 (327,680 tris) + 2-tri ground plane, 1920x1080, 2048^2 shadow map, "
                   "NormalMap + shadow, 1024^2 diffuse + normal map")
+SOUP_WORKLOAD = ("triangle soup, 4,000,000 tris at 3840x2160, centroids uniform, lognormal edges (median 2 px), "
+                 "constant NDC depth U[0,1] (~8x depth complexity), 1% exact duplicates submitted later, flat shader")
 BATCH = 64          # requests per launch sequence (the server's max_batch)
 N_REQUESTS = 10000  # Poisson stream length
 SEED = 5
@@ -326,6 +328,7 @@ def run_ours(args, world, rank, local):
         out["serve"] = serve_poisson(rp, reqs, plain_fps, e2e["value"], args)
         out["frame_1080p"] = run_frame(args)
         out["batched_views_64"] = run_views(args)
+        out["depth_stress_4m"] = run_soup(args)
     rp.release()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(pool, tex, reqs, args.cpu_seconds)
@@ -393,6 +396,47 @@ def run_frame(args) -> dict:
            "kernel_ms": {k: round(statistics.mean(v), 4) for k, v in kms.items()},
            "roofline": roofline(kms, counts, "frame_1080p"), "counts": counts,
            "tuning": {k: getattr(hsr.get_tuning(), k) for k in ("tile", "warps_per_cta", "ctas_per_sm")}}
+    g.release()
+    hsr.set_tuning(tile=old.tile, warps_per_cta=old.warps_per_cta, ctas_per_sm=old.ctas_per_sm)
+    return res
+
+
+def run_soup(args) -> dict:
+    """The depth-order stress frame: 4M-triangle soup at 3840x2160 (lognormal edges, median
+    2 px, ~8x depth complexity, 1% equal-depth duplicates), flat shader; device time."""
+    import torch
+
+    import hsr
+    from hsr import frame as hframe
+    from hsr import scenes
+
+    fr = scenes.soup_frame()
+    g = hframe.GpuFrame(fr)
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    old = hsr.get_tuning()
+    tuned = hsr.autotune(g.descs, reps=2)
+    hsr.set_profiling(True)
+    for _ in range(3):
+        g.render()
+    ms, kms, t = [], {k: [] for k in hsr.KERNELS}, None
+    for _ in range(max(5, args.steps // 3)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        g.render()
+        t = hsr.last_timing()
+        ms.append(t["batch_ms"])
+        for k, v in t["kernel_ms"].items():
+            kms[k].append(v)
+    hsr.set_profiling(False)
+    counts = {k: int(t[k]) for k in ("faces", "vertices", "normals", "records", "bin_pairs", "pixels",
+                                     "shaded_pixels", "fragments", "clipped_faces")}
+    s = statistics.mean(ms) / 1000.0
+    res = {"workload": SOUP_WORKLOAD, "frames_per_s": round(1.0 / s, 2), "ms": round(s * 1000.0, 4),
+           "mtris_per_s": round(counts["faces"] / s / 1e6, 1),
+           "gfrags_per_s": round(counts["fragments"] / s / 1e9, 2),
+           "note": "Gfrag/s counts covered (pixel, triangle) pairs, each tested against the depth buffer",
+           "kernel_ms": {k: round(statistics.mean(v), 4) for k, v in kms.items()},
+           "roofline": roofline(kms, counts, "soup_4m_2160p"), "counts": counts, "tuning": tuned}
     g.release()
     hsr.set_tuning(tile=old.tile, warps_per_cta=old.warps_per_cta, ctas_per_sm=old.ctas_per_sm)
     return res

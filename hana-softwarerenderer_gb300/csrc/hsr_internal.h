@@ -1,7 +1,7 @@
 // hsr_internal.h — data layout shared by the host runtime and the sm_103a kernels.
 //
 // Pipeline of one launch sequence (a batch of views = draws):
-//   k_vertex  : SoA attribute streams -> clip / world position / world normal per view
+//   k_vertex  : SoA attribute streams -> screen vertex / world position / world normal per view
 //   k_setup   : per face: fast accept or homogeneous clip (graphics.cpp:132-161), then per
 //               fan triangle divide / cull / viewport / bbox (graphics.cpp:314-347) -> one
 //               64-byte RasterRec, plus per-tile counts (warp-aggregated atomics)
@@ -13,6 +13,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdint.h>
 
 #include "../../include/hsr.h"
@@ -68,38 +69,41 @@ struct __align__(16) Payload {
 };
 static_assert(sizeof(RasterRec) == 64, "RasterRec must stay 64 bytes");
 
-// Per-draw descriptor on the device.
-struct DView {
+// Per-draw descriptor on the device.  The fields every raster tile reads come first, in
+// one 128-byte line (the struct is 128-byte aligned); the rest is read by the vertex and
+// setup stages and by the shading of tiles that hold fragments.
+struct __align__(128) DView {
+  // target and tiles (read per raster tile)
+  uint32_t* color; float* depth; uint32_t* prim; int32_t W, H;
+  int32_t tile_base, tiles_x, tiles_y, ntiles;
+  int32_t shader;
+  uint32_t flags;       // HSR_DRAW_*
+  float clear_depth;
+  uint32_t clear_rgba;
+  // ordering inside the batch: views this one waits for (-1 = none)
+  int32_t dep0, dep1;
+  int32_t has_dependents;  // another view of the batch waits for this one's tiles
+  uint32_t prim_base;
   // mesh (device)
   const float* px; const float* py; const float* pz;   // positions, SoA, padded to 4
   const float* nx; const float* ny; const float* nz;   // normals, SoA, padded to 4
   const float2* uv;
   const int4* fv; const int4* fvt; const int4* fvn;    // per-face corner indices (+pad)
   int32_t npos, nnrm, nuv, nfaces;
+  int32_t unified;  // every face corner has equal v, vt and vn indices (fvt, fvn unused)
   // vertex outputs (scratch)
-  float4* clip;   // [npos]
+  float4* sv;     // [npos] screen vertex: (x/w, y/w, z/w, 1/w) or plane mask (k_vertex)
   float4* wpos;   // [npos] or null
   float4* wnrm;   // [nnrm] (xyz, intensity) or null
   // shading
-  int32_t shader;
-  uint32_t flags;       // HSR_DRAW_*
   float mvp[16];        // camera_vp*model (light_vp*model for SHADOW), host-computed
   hsr_shader_data u;
   const uint32_t* diffuse; int32_t dw, dh, dbpp;
   const uint32_t* normal;  int32_t nw, nh, nbpp;
-  // target
-  uint32_t* color; float* depth; uint32_t* prim; int32_t W, H;
   // shadow map (colour plane of another target), null when ShaderData::shadow_map is null
   const uint32_t* sm_color; int32_t smW, smH;
-  // ordering inside the batch: views this one waits for (-1 = none)
-  int32_t dep0, dep1;
-  // tiles
-  int32_t tile_base, tiles_x, tiles_y, ntiles;
-  uint32_t prim_base;
-  float clear_depth;
-  uint32_t clear_rgba;
-  int32_t has_dependents;  // another view of the batch waits for this one's tiles
 };
+static_assert(offsetof(DView, prim_base) + sizeof(uint32_t) <= 128, "per-tile fields must share one line");
 
 struct Ctl {
   uint32_t rec_count;
@@ -111,6 +115,7 @@ struct Ctl {
   uint32_t big_count;      // triangles queued for sub-record expansion
   uint32_t post_next;      // work counter of k_post
   unsigned long long shaded_px;  // pixels whose winner was shaded by the raster
+  unsigned long long frag_px;    // covered (pixel, triangle) pairs the raster depth-tested
 };
 
 // A triangle whose bounding box touches more than kMaxRecordTiles tiles, queued by setup

@@ -80,6 +80,7 @@ static int noalloc_draw(Runtime* rt, const hsr_draw_desc& d) {
   v.uv = m->uv;
   v.fv = m->fv; v.fvt = m->fvt; v.fvn = m->fvn;
   v.npos = m->npos; v.nnrm = m->nnrm; v.nuv = m->nuv; v.nfaces = m->nfaces;
+  v.unified = m->unified ? 1 : 0;
   v.shader = d.shader;
   v.flags = d.flags;
   v.u = *d.uniforms;
@@ -141,7 +142,7 @@ static int noalloc_draw(Runtime* rt, const hsr_draw_desc& d) {
   if (host_bytes + sizeof(Ctl) > kStaticHostBytes)
     return fail(HSR_ERR_INVALID_ARG, "draw_noalloc: too many work chunks for the static staging array");
 
-  v.clip = (float4*)(dev + o_clip);
+  v.sv = (float4*)(dev + o_clip);
   v.wpos = needs_wpos_h(d.shader) ? (float4*)(dev + o_wpos) : nullptr;
   v.wnrm = wnrm ? (float4*)(dev + o_wnrm) : nullptr;
 
@@ -181,7 +182,7 @@ static int noalloc_draw(Runtime* rt, const hsr_draw_desc& d) {
   if (e != cudaSuccess) return cuda_fail(e, "draw_noalloc: clear counters");
   int kr = launch_vertex(dview, (const Chunk*)(dev + o_vch), (int)nvch, s);
   if (!kr) kr = launch_setup(dview, (const Chunk*)(dev + o_sch), (int)nsch, T, sc, s);
-  if (!kr) kr = launch_post(dview, T, sc, rt->num_sms * 2, s);
+  if (!kr) kr = launch_post(dview, T, sc, rt->num_sms * 4, s);
   if (!kr) kr = launch_big(dview, T, sc, rt->num_sms * 2, s);
   if (!kr) kr = launch_scan(sc, s);
   if (!kr) kr = launch_scatter(dview, T, sc, (int)std::max<size_t>((rec_cap + 255) / 256, 1), s);

@@ -199,6 +199,7 @@ int Runtime::plan_build(const hsr_draw_desc* descs, int n, Plan& p) {
     v.uv = m->uv;
     v.fv = m->fv; v.fvt = m->fvt; v.fvn = m->fvn;
     v.npos = m->npos; v.nnrm = m->nnrm; v.nuv = m->nuv; v.nfaces = m->nfaces;
+    v.unified = m->unified ? 1 : 0;
     v.shader = d.shader;
     v.flags = d.flags;
     v.u = *d.uniforms;
@@ -293,7 +294,7 @@ void Plan::bind(char* dev_base, char* host_base) {
   host = host_base;
   for (int k = 0; k < n; k++) {
     DView& v = views[k];
-    v.clip = (float4*)(dev + o_vout + offs[k].clip);
+    v.sv = (float4*)(dev + o_vout + offs[k].clip);
     v.wpos = shader_needs_wpos(v.shader) ? (float4*)(dev + o_vout + offs[k].wpos) : nullptr;
     v.wnrm = shader_needs_wnrm(v.shader) ? (float4*)(dev + o_vout + offs[k].wnrm) : nullptr;
   }
@@ -330,7 +331,7 @@ int Plan::enqueue(cudaStream_t s, int num_sms, const hsr_tuning& tu, cudaEvent_t
   if (ev && ev[2]) cudaEventRecord(ev[2], s);
   kr = launch_setup(dviews, (const Chunk*)(dev + o_sch), (int)schunks.size(), tile, sc, s);
   if (kr) return cuda_fail((cudaError_t)kr, "setup kernel");
-  kr = launch_post(dviews, tile, sc, num_sms * 2, s);
+  kr = launch_post(dviews, tile, sc, num_sms * 4, s);
   if (kr) return cuda_fail((cudaError_t)kr, "post kernel");
   kr = launch_big(dviews, tile, sc, num_sms * 2, s);
   if (kr) return cuda_fail((cudaError_t)kr, "big-triangle kernel");
@@ -373,6 +374,7 @@ void Runtime::record_result(const Plan& p, const Ctl& c) {
   timing.records = c.rec_count;
   timing.bin_pairs = c.bin_total;
   timing.shaded_pixels = c.shaded_px;
+  timing.fragments = c.frag_px;
   timing.pixels = p.total_pixels;
   timing.faces = p.total_faces;
   timing.vertices = p.total_pos;
@@ -553,12 +555,15 @@ int hsr_mesh_upload(const float* pos, int32_t npos, const float* nrm, int32_t nn
   if (rc == HSR_OK) {
     const size_t F = (size_t)std::max(nfaces, 1);
     std::vector<int4> fv(F), ft(F), fn(F);
+    bool unified = true;
     for (int i = 0; i < nfaces; i++) {
       const int32_t* f = faces + (size_t)i * 9;
       fv[i] = make_int4(f[0], f[3], f[6], 0);
       ft[i] = make_int4(f[1], f[4], f[7], 0);
       fn[i] = make_int4(f[2], f[5], f[8], 0);
+      for (int k = 0; k < 9; k += 3) unified = unified && f[k] == f[k + 1] && f[k] == f[k + 2];
     }
+    m->unified = unified;
     int4** dsts[3] = {&m->fv, &m->fvt, &m->fvn};
     std::vector<int4>* srcs[3] = {&fv, &ft, &fn};
     for (int k = 0; k < 3 && rc == HSR_OK; k++) {

@@ -18,6 +18,7 @@ struct MeshObj {  // Model (model.h:8-33) resident on the device
   float2* uv = nullptr;
   int4 *fv = nullptr, *fvt = nullptr, *fvn = nullptr;
   int32_t npos = 0, nnrm = 0, nuv = 0, nfaces = 0;
+  bool unified = false;  // v, vt and vn indices agree at every face corner
   ~MeshObj();
 };
 

@@ -4,11 +4,15 @@
 // vertex shader is a pure function of its a2v inputs, and each output stream depends on
 // one attribute stream only (clip and world position on `v`, world normal and light
 // intensity on `vn`, uv passes through), so each attribute is transformed once and the
-// setup kernel gathers per corner: the same bits as three vertex() calls per face.
+// setup kernel gathers per corner: the same bits as three vertex() calls per face.  The
+// per-corner work of rasterize_triangle that depends on one vertex alone — the visibility
+// test of clip_triangle's fast accept (graphics.cpp:132-134, 140-142) and, for a visible
+// vertex, the perspective divide and 1/w (:320-337) — is done here once per vertex too
+// (the screen vertex, see screen_vertex), so setup divides nothing on the fast path.
 //
-// k_setup follows graphics.cpp:136-161 (clip) and :314-347 (divide, cull, viewport,
-// bounding box) for every fan triangle and emits one RasterRec.  Faces that fail the fast
-// accept are clipped by the whole warp: lane k carries varying k of the polygon through
+// k_setup follows graphics.cpp:136-161 (clip) and :314-347 (cull, viewport, bounding box)
+// for every fan triangle and emits one RasterRec.  Faces that fail the fast accept are
+// clipped by the whole warp: lane k carries varying k of the polygon through
 // Sutherland-Hodgman while every lane evaluates the plane tests on the clip coordinates.
 #include <float.h>
 
@@ -17,6 +21,66 @@
 namespace hsr {
 
 constexpr unsigned kFull = 0xffffffffu;
+
+// ---------------------------------------------------------------------------------------
+// clip-space helpers
+// ---------------------------------------------------------------------------------------
+enum { PW, PX, NX, PY, NY, PZ, NZ };
+
+// is_inside_plane (graphics.cpp:29-49) on clip coordinates c[0..3]
+__device__ __forceinline__ bool inside_plane(const float* c, int plane) {
+  switch (plane) {
+    case PW: return c[3] >= 1e-5f;
+    case PX: return c[0] <= c[3];
+    case NX: return c[0] >= -c[3];
+    case PY: return c[1] <= c[3];
+    case NY: return c[1] >= -c[3];
+    case PZ: return c[2] <= c[3];
+    default: return c[2] >= -c[3];
+  }
+}
+// get_intersect_ratio (graphics.cpp:51-71)
+__device__ __forceinline__ float intersect_ratio(const float* p, const float* q, int plane) {
+  switch (plane) {
+    case PW: return fd(fs(p[3], 1e-5f), fs(p[3], q[3]));
+    case PX: return fd(fs(p[3], p[0]), fs(fs(p[3], p[0]), fs(q[3], q[0])));
+    case NX: return fd(fa(p[3], p[0]), fs(fa(p[3], p[0]), fa(q[3], q[0])));
+    case PY: return fd(fs(p[3], p[1]), fs(fs(p[3], p[1]), fs(q[3], q[1])));
+    case NY: return fd(fa(p[3], p[1]), fs(fa(p[3], p[1]), fa(q[3], q[1])));
+    case PZ: return fd(fs(p[3], p[2]), fs(fs(p[3], p[2]), fs(q[3], q[2])));
+    default: return fd(fa(p[3], p[2]), fs(fa(p[3], p[2]), fa(q[3], q[2])));
+  }
+}
+__device__ __forceinline__ bool vertex_visible(float4 c) {  // is_vertex_visible (:132-134)
+  return fabsf(c.x) <= c.w && fabsf(c.y) <= c.w && fabsf(c.z) <= c.w;
+}
+
+// Clip position of vertex i of a view: ObjectToClipPos (IShader.h:55-61), the bits k_vertex
+// computed for it.
+__device__ __forceinline__ float4 clip_of(const DView& v, int i) {
+  return mat_vec(v.mvp, __ldg(v.px + i), __ldg(v.py + i), __ldg(v.pz + i), 1.f);
+}
+
+// Screen vertex of one clip position.  A vertex that is visible (is_vertex_visible,
+// graphics.cpp:132-134) with w >= 1e-5 stores what rasterize_triangle derives from it
+// alone: (x/w, y/w, z/w, 1/w) (graphics.cpp:321-323, 335-337); its |x/w| is <= 1 or NaN.
+// Any other vertex stores (kSvSpecial, mask, 0, 0), bit p of the mask being
+// is_inside_plane for plane p in the clipper's order (W, +X, -X, +Y, -Y, +Z, -Z) and bit 7
+// is_vertex_visible.  A normal screen vertex is inside every plane (|x|,|y|,|z| <= w and
+// w >= 1e-5), so its mask is 0xff.
+constexpr float kSvSpecial = 4.0f;
+__device__ __forceinline__ float4 screen_vertex(float4 c) {
+  const bool vis = vertex_visible(c);
+  if (vis && c.w >= 1e-5f) return make_float4(fd(c.x, c.w), fd(c.y, c.w), fd(c.z, c.w), fd(1.f, c.w));
+  const float a[4] = {c.x, c.y, c.z, c.w};
+  uint32_t m = vis ? 0x80u : 0u;
+#pragma unroll
+  for (int p = PW; p <= NZ; p++)
+    if (inside_plane(a, p)) m |= 1u << p;
+  return make_float4(kSvSpecial, __uint_as_float(m), 0.f, 0.f);
+}
+__device__ __forceinline__ bool sv_normal(float4 s) { return !(fabsf(s.x) > 1.f); }
+__device__ __forceinline__ uint32_t sv_mask(float4 s) { return sv_normal(s) ? 0xffu : __float_as_uint(s.y); }
 
 // ---------------------------------------------------------------------------------------
 // vertex stage
@@ -35,7 +99,7 @@ __global__ void __launch_bounds__(256) k_vertex(const DView* __restrict__ views,
 #pragma unroll
     for (int k = 0; k < 4; k++) {
       if (i4 + k >= ch.end) break;
-      v.clip[i4 + k] = mat_vec(v.mvp, xs[k], ys[k], zs[k], 1.f);
+      v.sv[i4 + k] = screen_vertex(mat_vec(v.mvp, xs[k], ys[k], zs[k], 1.f));
       if (v.wpos) {
         float4 w = mat_vec(v.u.model_matrix, xs[k], ys[k], zs[k], 1.f);
         v.wpos[i4 + k] = make_float4(w.x, w.y, w.z, 0.f);
@@ -78,12 +142,13 @@ __device__ __forceinline__ bool coord_ok(float c) {
   return (a == 0.f) || (a >= 0x1p-8f && a <= 0x1p20f);
 }
 
-// Divide, cull, viewport, bounding box of one fan triangle (graphics.cpp:314-347).
-__device__ __forceinline__ bool build_rec(const DView& v, float4 c0, float4 c1, float4 c2, uint32_t seq,
-                                          uint32_t view, RasterRec& r) {
-  const F3 n0 = {fd(c0.x, c0.w), fd(c0.y, c0.w), fd(c0.z, c0.w)};
-  const F3 n1 = {fd(c1.x, c1.w), fd(c1.y, c1.w), fd(c1.z, c1.w)};
-  const F3 n2 = {fd(c2.x, c2.w), fd(c2.y, c2.w), fd(c2.z, c2.w)};
+// Perspective divide of rasterize_triangle (graphics.cpp:321-323): clip / w per component.
+__device__ __forceinline__ F3 ndc_of(float4 c) { return {fd(c.x, c.w), fd(c.y, c.w), fd(c.z, c.w)}; }
+
+// Cull, viewport, bounding box of one fan triangle from its corners' NDC coordinates
+// (graphics.cpp:324-347).
+__device__ __forceinline__ bool build_rec(const DView& v, F3 n0, F3 n1, F3 n2, uint32_t seq, uint32_t view,
+                                          RasterRec& r) {
   // is_back_facing (:172-180), evaluated left to right
   float sa = fs(fm(n0.x, n1.y), fm(n0.y, n1.x));
   sa = fa(sa, fm(n1.x, n2.y));
@@ -206,6 +271,34 @@ __device__ __forceinline__ uint32_t warp_reserve(bool want, uint32_t* counter) {
   return want ? base + (uint32_t)__popc(m & ((1u << lane) - 1u)) : ~0u;
 }
 
+// Slot of this thread's item when `want`, one atomicAdd per block (~0u otherwise).  Every
+// thread of the block calls this.  All warps of the grid append to one counter, and a
+// returning atomic on a single address is served one at a time: reserving per block
+// instead of per warp divides those atomics by the warps of a block.
+template <int THREADS>
+__device__ __forceinline__ uint32_t block_reserve(bool want, uint32_t* counter) {
+  __shared__ uint32_t s_count[THREADS / 32];
+  __shared__ uint32_t s_base;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned m = __ballot_sync(kFull, want);
+  if (lane == 0) s_count[warp] = (uint32_t)__popc(m);
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t c = lane < THREADS / 32 ? s_count[lane] : 0u;
+    uint32_t incl = c;
+#pragma unroll
+    for (int o = 1; o < THREADS / 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFull, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const uint32_t total = __shfl_sync(kFull, incl, THREADS / 32 - 1);
+    if (lane < THREADS / 32) s_count[lane] = incl - c;
+    if (lane == 0) s_base = total ? atomicAdd(counter, total) : 0u;
+  }
+  __syncthreads();
+  return want ? s_base + s_count[warp] + (uint32_t)__popc(m & ((1u << lane) - 1u)) : ~0u;
+}
+
 // Store the records of a warp at their reserved slots (at most one per lane, each touching
 // <= kMaxRecordTiles tiles) and count the tiles they touch, aggregating equal tiles across
 // lanes.  All 32 lanes call this.
@@ -232,49 +325,19 @@ __device__ void append_small(bool valid, uint32_t slot, const RasterRec& r, cons
   }
 }
 
-enum { PW, PX, NX, PY, NY, PZ, NZ };
-
-// is_inside_plane (graphics.cpp:29-49) on clip coordinates c[0..3]
-__device__ __forceinline__ bool inside_plane(const float* c, int plane) {
-  switch (plane) {
-    case PW: return c[3] >= 1e-5f;
-    case PX: return c[0] <= c[3];
-    case NX: return c[0] >= -c[3];
-    case PY: return c[1] <= c[3];
-    case NY: return c[1] >= -c[3];
-    case PZ: return c[2] <= c[3];
-    default: return c[2] >= -c[3];
-  }
-}
-// get_intersect_ratio (graphics.cpp:51-71)
-__device__ __forceinline__ float intersect_ratio(const float* p, const float* q, int plane) {
-  switch (plane) {
-    case PW: return fd(fs(p[3], 1e-5f), fs(p[3], q[3]));
-    case PX: return fd(fs(p[3], p[0]), fs(fs(p[3], p[0]), fs(q[3], q[0])));
-    case NX: return fd(fa(p[3], p[0]), fs(fa(p[3], p[0]), fa(q[3], q[0])));
-    case PY: return fd(fs(p[3], p[1]), fs(fs(p[3], p[1]), fs(q[3], q[1])));
-    case NY: return fd(fa(p[3], p[1]), fs(fa(p[3], p[1]), fa(q[3], q[1])));
-    case PZ: return fd(fs(p[3], p[2]), fs(fs(p[3], p[2]), fs(q[3], q[2])));
-    default: return fd(fa(p[3], p[2]), fs(fa(p[3], p[2]), fa(q[3], q[2])));
-  }
-}
-__device__ __forceinline__ bool vertex_visible(float4 c) {  // is_vertex_visible (:132-134)
-  return fabsf(c.x) <= c.w && fabsf(c.y) <= c.w && fabsf(c.z) <= c.w;
-}
-
 // True when the reference's clipper returns 0 vertices for this face without creating any
 // new vertex: Sutherland-Hodgman copies a polygon whose vertices are all inside a plane
 // unchanged, so if the three corners pass every plane before some plane (in the order
 // W, +X, -X, +Y, -Y, +Z, -Z of graphics.cpp:152-158) and all fail that plane, that stage
 // emits nothing and the face is dropped (CLIP_IN2OUT / CLIP_OUT2IN return 0).  Faces whose
-// corners straddle a plane first go to the full clipper.
-__device__ __forceinline__ bool clip_trivially_empty(float4 c0, float4 c1, float4 c2) {
-  const float a[4] = {c0.x, c0.y, c0.z, c0.w}, b[4] = {c1.x, c1.y, c1.z, c1.w}, c[4] = {c2.x, c2.y, c2.z, c2.w};
+// corners straddle a plane first go to the full clipper.  m0..m2 are the corners' plane
+// masks (see screen_vertex).
+__device__ __forceinline__ bool clip_trivially_empty(uint32_t m0, uint32_t m1, uint32_t m2) {
 #pragma unroll
   for (int plane = PW; plane <= NZ; plane++) {
-    const bool ia = inside_plane(a, plane), ib = inside_plane(b, plane), ic = inside_plane(c, plane);
-    if (!ia && !ib && !ic) return true;
-    if (!(ia && ib && ic)) return false;
+    const uint32_t all = (m0 & m1 & m2) >> plane & 1u, any = (m0 | m1 | m2) >> plane & 1u;
+    if (!any) return true;
+    if (!all) return false;
   }
   return false;
 }
@@ -296,38 +359,59 @@ __global__ void __launch_bounds__(kSetupThreads, 4) k_setup(const DView* __restr
   Payload pl;
   if (active) {
     const int4 iv = __ldg(&v.fv[f]);
-    const float4 c0 = v.clip[iv.x], c1 = v.clip[iv.y], c2 = v.clip[iv.z];
-    if (vertex_visible(c0) && vertex_visible(c1) && vertex_visible(c2)) {
-      valid = build_rec(v, c0, c1, c2, (uint32_t)f << 4, (uint32_t)ch.view, r);
-      if (valid && payload_f4(v.shader) > 0) {
-        // corner varyings of the three vertex() calls, in shader_struct_v2f order
-        float c[3][kVaryings];
-        const int pi[3] = {iv.x, iv.y, iv.z};
-        const float4 cl[3] = {c0, c1, c2};
-        int4 it = make_int4(0, 0, 0, 0), in = make_int4(0, 0, 0, 0);
-        if (v.uv) it = __ldg(&v.fvt[f]);
-        if (v.wnrm) in = __ldg(&v.fvn[f]);
+    const int pi[3] = {iv.x, iv.y, iv.z};
+    float4 sv[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) sv[k] = __ldg(&v.sv[pi[k]]);
+    bool accept = sv_normal(sv[0]) && sv_normal(sv[1]) && sv_normal(sv[2]);
+    if (!accept) {
+      const uint32_t m0 = sv_mask(sv[0]), m1 = sv_mask(sv[1]), m2 = sv_mask(sv[2]);
+      if (m0 & m1 & m2 & 0x80u) {
+        // all three visible, one with w < 1e-5: fast accept, divide here
+        accept = true;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          const float4 c = clip_of(v, pi[k]);
+          const F3 n = ndc_of(c);
+          sv[k] = make_float4(n.x, n.y, n.z, fd(1.f, c.w));
+        }
+      } else {
+        needs_clip = !clip_trivially_empty(m0, m1, m2);
+      }
+    }
+    if (accept) {
+      valid = build_rec(v, {sv[0].x, sv[0].y, sv[0].z}, {sv[1].x, sv[1].y, sv[1].z}, {sv[2].x, sv[2].y, sv[2].z},
+                        (uint32_t)f << 4, (uint32_t)ch.view, r);
+      const int nf4 = payload_f4(v.shader);
+      if (valid && nf4 > 0) {
+        // corner varyings of the three vertex() calls (Payload layout)
+        int4 it = iv, in = iv;  // meshes whose v, vt and vn indices agree skip two loads
+        if (!v.unified) {
+          if (v.uv && nf4 >= 3) it = __ldg(&v.fvt[f]);
+          if (v.wnrm) in = __ldg(&v.fvn[f]);
+        }
         const int ti[3] = {it.x, it.y, it.z}, ni[3] = {in.x, in.y, in.z};
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-          c[k][0] = cl[k].x; c[k][1] = cl[k].y; c[k][2] = cl[k].z; c[k][3] = cl[k].w;
-          const float4 wp = v.wpos ? v.wpos[pi[k]] : make_float4(0.f, 0.f, 0.f, 0.f);
-          const float4 wn = v.wnrm ? v.wnrm[ni[k]] : make_float4(0.f, 0.f, 0.f, 0.f);
-          const float2 t = (v.uv && payload_f4(v.shader) >= 3) ? __ldg(&v.uv[ti[k]]) : make_float2(0.f, 0.f);
-          c[k][4] = wp.x; c[k][5] = wp.y; c[k][6] = wp.z;
-          c[k][7] = wn.x; c[k][8] = wn.y; c[k][9] = wn.z;
-          c[k][10] = t.x; c[k][11] = t.y; c[k][12] = wn.w;
+          const float4 wp = v.wpos ? __ldg(&v.wpos[pi[k]]) : make_float4(0.f, 0.f, 0.f, 0.f);
+          const float4 wn = v.wnrm ? __ldg(&v.wnrm[ni[k]]) : make_float4(0.f, 0.f, 0.f, 0.f);
+          const float2 t = (v.uv && nf4 >= 3) ? __ldg(&v.uv[ti[k]]) : make_float2(0.f, 0.f);
+          pl.f[k] = sv[k].w;  // recip_w (graphics.cpp:333-337)
+          pl.f[3 + k] = v.shader == HSR_SHADER_SHADOW ? clip_of(v, pi[k]).z : wn.w;
+          pl.f[6 + 2 * k] = t.x;
+          pl.f[7 + 2 * k] = t.y;
+          pl.f[12 + 3 * k] = wn.x; pl.f[13 + 3 * k] = wn.y; pl.f[14 + 3 * k] = wn.z;
+          pl.f[21 + 3 * k] = wp.x; pl.f[22 + 3 * k] = wp.y; pl.f[23 + 3 * k] = wp.z;
         }
-        make_payload(v.shader, c[0], c[1], c[2], pl);
+        pl.f[30] = 0.f;
+        pl.f[31] = 0.f;
       }
-    } else {
-      needs_clip = !clip_trivially_empty(c0, c1, c2);
     }
   }
   int tx0, ty0, ntw, nt = 0;
   if (valid) rec_tiles(r, T, tx0, ty0, ntw, nt);
   const bool big = valid && nt > kMaxRecordTiles;
-  const uint32_t slot = warp_reserve(valid && !big, &sc.ctl->rec_count);
+  const uint32_t slot = block_reserve<kSetupThreads>(valid && !big, &sc.ctl->rec_count);
   append_small(valid && !big, slot, r, pl, payload_f4(v.shader), v, T, sc);
 
   // huge triangles and faces that need the clipper are queued for k_post, which spreads
@@ -359,7 +443,7 @@ __device__ void clip_face(const DView& v, int view, int face, int T, const Scrat
     const int ti = lane == 0 ? it.x : (lane == 1 ? it.y : it.z);
     const int ni = lane == 0 ? in.x : (lane == 1 ? in.y : in.z);
     float* o = A + lane * kPolyStride;
-    const float4 c = v.clip[pi];
+    const float4 c = clip_of(v, pi);
     o[0] = c.x; o[1] = c.y; o[2] = c.z; o[3] = c.w;
     const float4 wp = v.wpos ? v.wpos[pi] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 wn = v.wnrm ? v.wnrm[ni] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -399,8 +483,8 @@ __device__ void clip_face(const DView& v, int view, int face, int T, const Scrat
     const float* p0 = src;
     const float* p1 = src + (lane + 1) * kPolyStride;
     const float* p2 = src + (lane + 2) * kPolyStride;
-    valid = build_rec(v, make_float4(p0[0], p0[1], p0[2], p0[3]), make_float4(p1[0], p1[1], p1[2], p1[3]),
-                      make_float4(p2[0], p2[1], p2[2], p2[3]), ((uint32_t)face << 4) | ((uint32_t)lane << 1) | 1u,
+    valid = build_rec(v, ndc_of(make_float4(p0[0], p0[1], p0[2], p0[3])), ndc_of(make_float4(p1[0], p1[1], p1[2], p1[3])),
+                      ndc_of(make_float4(p2[0], p2[1], p2[2], p2[3])), ((uint32_t)face << 4) | ((uint32_t)lane << 1) | 1u,
                       (uint32_t)view, r);
     if (valid) make_payload(v.shader, p0, p1, p2, pl);
   }
@@ -424,19 +508,27 @@ __device__ void clip_face(const DView& v, int view, int face, int T, const Scrat
 
 constexpr int kPostThreads = 256;
 
-// Drains the clip queue of k_setup, one warp per face.
-__global__ void __launch_bounds__(kPostThreads) k_post(const DView* __restrict__ views, int T, Scratch sc) {
+// Drains the clip queue of k_setup, one warp per face.  Faces are claimed one ahead, so the
+// claim's round trip overlaps the current face; the grid fills every SM (the queue is short
+// and each face is a chain of dependent loads, so resident warps set the throughput).
+__global__ void __launch_bounds__(kPostThreads, 4) k_post(const DView* __restrict__ views, int T, Scratch sc) {
   __shared__ float poly[kPostThreads / 32][2][16 * kPolyStride];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (sc.ctl->error & kErrCapacity) return;
   const uint32_t nclip = min(sc.ctl->clip_count, sc.clip_cap);
+  uint32_t item = 0, ahead = 0;
+  if (lane == 0) {
+    item = atomicAdd(&sc.ctl->post_next, 1u);
+    ahead = item < nclip ? atomicAdd(&sc.ctl->post_next, 1u) : nclip;
+  }
+  item = __shfl_sync(kFull, item, 0);
   for (;;) {
-    uint32_t item = 0;
-    if (lane == 0) item = atomicAdd(&sc.ctl->post_next, 1u);
-    item = __shfl_sync(kFull, item, 0);
     if (item >= nclip) break;
+    const uint32_t next = __shfl_sync(kFull, ahead, 0);
+    if (lane == 0) ahead = next < nclip ? atomicAdd(&sc.ctl->post_next, 1u) : nclip;
     const int2 vf = sc.clipq[item];
     clip_face(views[vf.x], vf.x, vf.y, T, sc, poly[warp][0], poly[warp][1]);
+    item = next;
   }
 }
 

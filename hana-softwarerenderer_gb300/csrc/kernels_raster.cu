@@ -30,11 +30,16 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr long kWaitLimit = 1L << 23;  // ~1-2 s of polling before a dependency wait gives up
 constexpr uint32_t kNone = 0xffffffffu;
 
-__device__ __forceinline__ int find_view(const DView* views, int nviews, int t) {
+constexpr int kSharedViews = 256;  // views whose first tile index the raster keeps in shared memory
+
+// View owning tile t: the last view whose first tile is <= t (views hold consecutive tile
+// ranges in batch order).  `tbase` is the shared copy when the batch has at most
+// kSharedViews views, else null and the descriptors are searched in global memory.
+__device__ __forceinline__ int find_view(const DView* views, const int32_t* tbase, int nviews, int t) {
   int lo = 0, hi = nviews - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    if (views[mid].tile_base <= t) lo = mid; else hi = mid - 1;
+    if ((tbase ? tbase[mid] : views[mid].tile_base) <= t) lo = mid; else hi = mid - 1;
   }
   return lo;
 }
@@ -74,18 +79,18 @@ __constant__ uint32_t kDivMagic[33] = {0,     65536, 32768, 21846, 16384, 13108,
                                        5958,  5462,  5042,  4682,  4370,  4096,  3856,  3641, 3450, 3277, 3121,
                                        2979,  2850,  2731,  2622,  2521,  2428,  2341,  2260, 2185, 2115, 2048};
 
-// Per-warp tile state in shared memory: key (ordered depth | submission), and for the
-// winner its payload index, seq and barycentric weights.
+// Per-warp tile state in shared memory: per pixel the key (ordered depth | submission) and
+// the index of the record that holds it.
 template <int NPIX>
 struct TileState {
   unsigned long long key[NPIX];
-  uint32_t pay[NPIX];
-  uint32_t seq[NPIX];
-  float b0[NPIX], b1[NPIX], b2[NPIX];
+  uint32_t rec[NPIX];
 };
 
 // Shade the winners of one tile and write colour, depth and prim id (fused clear writes the
-// clear values where nothing won).  S is the shader, known at compile time.
+// clear values where nothing won).  S is the shader, known at compile time.  The winner's
+// barycentric weights are evaluated again from its record: the same operations on the same
+// values as in the visibility pass, so the same bits.
 template <int T, int S>
 __device__ __forceinline__ uint32_t shade_tile(const DView& v, const Scratch& sc, const TileState<T * T>& st, int ox,
                                                int oy, bool clear, const ByteTables& bt) {
@@ -99,19 +104,22 @@ __device__ __forceinline__ uint32_t shade_tile(const DView& v, const Scratch& sc
     const int x = ox + p % T, y = oy + p / T;
     if (x >= v.W || y >= v.H) continue;
     const size_t idx = (size_t)y * v.W + x;
-    const uint32_t pi = st.pay[p];
-    if (pi != kNone) {
+    const uint32_t ri = st.rec[p];
+    if (ri != kNone) {
       shaded++;
+      const RasterRec r = sc.recs[ri];
+      float b0, b1, b2;
+      cover_test(r.ax, r.ay, r.e1x, r.e1y, r.e2x, r.e2y, r.uz, ((r.view >> kRecFlagShift) & kRecExact) != 0u, (float)x,
+                 (float)y, b0, b1, b2);
       float P[NF4 > 0 ? NF4 * 4 : 4];
       if constexpr (NF4 > 0) {
-        const float4* src = reinterpret_cast<const float4*>(&sc.pay[pi]);
+        const float4* src = reinterpret_cast<const float4*>(&sc.pay[r.pad]);
 #pragma unroll
         for (int k = 0; k < NF4; k++) reinterpret_cast<float4*>(P)[k] = src[k];
       }
-      const uint32_t seq = st.seq[p];
-      const uint32_t prim = v.prim_base + (seq >> 4) + 1u;
+      const uint32_t prim = v.prim_base + (r.seq >> 4) + 1u;
       const uint32_t alpha = clear ? v.clear_rgba : __ldcg(&v.color[idx]);
-      v.color[idx] = pack_rgb(fragment_s<S>(v, P, st.b0[p], st.b1[p], st.b2[p], prim, bt), alpha);
+      v.color[idx] = pack_rgb(fragment_s<S>(v, P, b0, b1, b2, prim, bt), alpha);
       v.depth[idx] = from_ord((uint32_t)(st.key[p] >> 32));
       if (v.prim) v.prim[idx] = prim;
     } else if (clear) {
@@ -124,25 +132,31 @@ __device__ __forceinline__ uint32_t shade_tile(const DView& v, const Scratch& sc
 }
 
 // One warp per screen tile.  For each batch of 32 records of the tile list, every record's
-// bounding-box pixels inside the tile form a run of candidates; the runs are laid end to
-// end (warp prefix sum) and the lanes walk the candidates 32 at a time, so the work is
-// proportional to the pixels the triangles can touch rather than to records x 32 lanes.
-// A covered candidate resolves visibility with a 64-bit atomicMin on
+// bounding-box pixels inside the tile form a run of candidates; the non-empty runs are
+// compacted and laid end to end (warp prefix sum) and the lanes walk the candidates 32 at
+// a time, so the work is proportional to the pixels the triangles can touch rather than
+// to records x 32 lanes.  The run owning a candidate is found from a ballot of the runs
+// starting in the current window of 32 candidates.  A covered candidate resolves
+// visibility with a 64-bit atomicMin on
 //     (ordered depth << 32) | (0xfffffffe - seq)
 // in shared memory: smallest depth first, and among equal depths the later submission.
 // The lane whose key is still the minimum after the warp's atomics records the winner's
-// payload, seq and weights (two lanes of one step never hold the same key: one triangle
-// covers a pixel once).  Shading then runs once per pixel with a winner.
+// record (two lanes of one step never hold the same key: one triangle covers a pixel
+// once).  Shading then runs once per pixel with a winner.
 template <int T, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* __restrict__ views, Scratch sc) {
   constexpr int NPIX = T * T;
   constexpr int PPL = NPIX / 32;
   __shared__ TileState<NPIX> sst[WARPS];
-  __shared__ RasterRec srec[WARPS][32];
-  __shared__ uint32_t soff[WARPS][32];
-  __shared__ uint32_t sbox[WARPS][32];
+  __shared__ RasterRec srec[WARPS][32];  // the batch's non-empty records, compacted (rsv = index)
+  __shared__ uint32_t soff[WARPS][32];   // first candidate of each
+  __shared__ uint32_t sbox[WARPS][32];   // box in the tile: x0 | y0 << 8 | width << 16
   __shared__ float s_u8f[256], s_u8n[256];
+  __shared__ int32_t s_tbase[kSharedViews];
   build_byte_tables(s_u8f, s_u8n);
+  const int32_t* tbase = sc.nviews <= kSharedViews ? s_tbase : nullptr;
+  if (tbase)
+    for (int i = threadIdx.x; i < sc.nviews; i += blockDim.x) s_tbase[i] = views[i].tile_base;
   __syncthreads();
   const ByteTables bt{s_u8f, s_u8n};
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -150,18 +164,36 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
   if (sc.ctl->error & kErrCapacity) return;
   const uint32_t nrec = min(sc.ctl->rec_count, sc.rec_cap);
 
-  uint32_t t = 0;
-  if (lane == 0) t = atomicAdd(&sc.ctl->tile_next, 1u);
+  // Tiles are handed out by one counter, two ahead: while a tile is rasterised, the next
+  // tile's list bounds are already loading and the one after it is being claimed, so neither
+  // the counter's round trip nor the list lookup waits on the critical path (dependencies
+  // only point to lower tile indices, so holding later tiles never blocks).
+  const uint32_t ntiles = (uint32_t)sc.ntiles;
+  uint32_t t = 0, t_ahead = 0;
+  if (lane == 0) {
+    t = atomicAdd(&sc.ctl->tile_next, 1u);
+    t_ahead = atomicAdd(&sc.ctl->tile_next, 1u);
+  }
   t = __shfl_sync(kFull, t, 0);
+  uint32_t n = 0, off = 0;
+  if (t < ntiles) {
+    n = sc.tile_count[t];
+    off = sc.tile_off[t];
+  }
   for (;;) {
-    if ((int)t >= sc.ntiles) break;
-    // grab the next tile now, use it after this one: the atomic's latency overlaps the work
-    // (dependencies only point to lower tile indices, so holding a later tile never blocks)
-    uint32_t t_next = 0;
-    if (lane == 0) t_next = atomicAdd(&sc.ctl->tile_next, 1u);
-    const uint32_t n = sc.tile_count[t];
-    const uint32_t off = sc.tile_off[t];
-    const int vi = find_view(views, sc.nviews, (int)t);
+    if (t >= ntiles) break;
+    const uint32_t t_next = __shfl_sync(kFull, t_ahead, 0);
+    if (lane == 0) t_ahead = t_next < ntiles ? atomicAdd(&sc.ctl->tile_next, 1u) : ntiles;
+    uint32_t n_next = 0, off_next = 0;
+    if (t_next < ntiles) {
+      n_next = sc.tile_count[t_next];
+      off_next = sc.tile_off[t_next];
+    }
+    if (t_next < ntiles) {  // warm L1 with the next tile's view descriptor line
+      const DView* vn = views + find_view(views, tbase, sc.nviews, (int)t_next);
+      asm volatile("prefetch.global.L1 [%0];" ::"l"(vn));
+    }
+    const int vi = find_view(views, tbase, sc.nviews, (int)t);
     const DView& v = views[vi];
     if (lane == 0) {
       wait_view(sc, views, v.dep0);
@@ -195,27 +227,24 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
         float d = v.clear_depth;
         if (!clear && x < v.W && y < v.H) d = __ldcg(&v.depth[(size_t)y * v.W + x]);
         st.key[p] = buffer_key(d);
-        st.pay[p] = kNone;
+        st.rec[p] = kNone;
       }
+      uint32_t frags = 0;  // covered candidates of this lane
       for (uint32_t b = 0; b < n; b += 32) {
         const uint32_t cnt = min(32u, n - b);
-        uint32_t c = 0;
-        __syncwarp();
+        uint32_t c = 0, box = 0, ri = kNone;
+        RasterRec rr;
         if ((uint32_t)lane < cnt) {
-          const uint32_t ri = sc.bins[off + b + (uint32_t)lane];
-          RasterRec rr;
-          if (ri < nrec) {
+          ri = sc.bins[off + b + (uint32_t)lane];
+          if (ri < nrec) {  // an index past the records never comes from a consistent bin pass
             rr = sc.recs[ri];
-          } else {  // never produced by a consistent bin pass: covers nothing
-            rr.xr = 1u; rr.yr = 1u; rr.seq = 0u; rr.view = 0u; rr.pad = kNone;
+            const int lx0 = max((int)(rr.xr & 0xffffu) - ox, 0), lx1 = min((int)(rr.xr >> 16) - ox, T - 1);
+            const int ly0 = max((int)(rr.yr & 0xffffu) - oy, 0), ly1 = min((int)(rr.yr >> 16) - oy, T - 1);
+            if (lx0 <= lx1 && ly0 <= ly1) {
+              c = (uint32_t)((lx1 - lx0 + 1) * (ly1 - ly0 + 1));
+              box = (uint32_t)lx0 | ((uint32_t)ly0 << 8) | ((uint32_t)(lx1 - lx0 + 1) << 16);
+            }
           }
-          const int lx0 = max((int)(rr.xr & 0xffffu) - ox, 0), lx1 = min((int)(rr.xr >> 16) - ox, T - 1);
-          const int ly0 = max((int)(rr.yr & 0xffffu) - oy, 0), ly1 = min((int)(rr.yr >> 16) - oy, T - 1);
-          if (lx0 <= lx1 && ly0 <= ly1) {
-            c = (uint32_t)((lx1 - lx0 + 1) * (ly1 - ly0 + 1));
-            sbox[warp][lane] = (uint32_t)lx0 | ((uint32_t)ly0 << 8) | ((uint32_t)(lx1 - lx0 + 1) << 16);
-          }
-          srec[warp][lane] = rr;
         }
         uint32_t incl = c;
 #pragma unroll
@@ -224,36 +253,42 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
           if (lane >= o) incl += y;
         }
         const uint32_t W = __shfl_sync(kFull, incl, 31);
-        soff[warp][lane] = incl - c;
+        const uint32_t start = incl - c;
+        const unsigned ne = __ballot_sync(kFull, c > 0u);
+        __syncwarp();
+        if (c > 0u) {  // compact the non-empty runs
+          const int k = __popc(ne & ((1u << lane) - 1u));
+          rr.rsv = ri;
+          srec[warp][k] = rr;
+          soff[warp][k] = start;
+          sbox[warp][k] = box;
+        }
         __syncwarp();
         for (uint32_t base = 0; base < W; base += 32) {
+          // runs starting before this window, and a bit per run starting inside it
+          const uint32_t before = (uint32_t)__popc(__ballot_sync(kFull, c > 0u && start < base));
+          const uint32_t here = __reduce_or_sync(
+              kFull, (c > 0u && start >= base && start - base < 32u) ? 1u << (start - base) : 0u);
           const uint32_t i = base + (uint32_t)lane;
           bool covered = false;
           unsigned long long key = 0ull, old = 0ull;
           int p = 0, j = 0;
-          float b0 = 0.f, b1 = 0.f, b2 = 0.f;
           if (i < W) {
-            // record j owning candidate i: the last j with soff[j] <= i (empty runs never win)
-            int lo = 0, hi = (int)cnt - 1;
-#pragma unroll
-            for (int s = 0; s < 5; s++) {
-              const int mid = (lo + hi + 1) >> 1;
-              if (lo < hi) {
-                if (soff[warp][mid] <= i) lo = mid; else hi = mid - 1;
-              }
-            }
-            j = lo;
+            // owner: the last run starting at or before candidate i
+            j = (int)(before + (uint32_t)__popc(here & ((2u << lane) - 1u))) - 1;
             const uint32_t q = i - soff[warp][j];
-            const uint32_t box = sbox[warp][j];
-            const uint32_t lw = box >> 16;
+            const uint32_t bx = sbox[warp][j];
+            const uint32_t lw = bx >> 16;
             const uint32_t qy = (q * kDivMagic[lw]) >> 16;
-            const int lx = (int)(box & 255u) + (int)(q - qy * lw);
-            const int ly = (int)((box >> 8) & 255u) + (int)qy;
+            const int lx = (int)(bx & 255u) + (int)(q - qy * lw);
+            const int ly = (int)((bx >> 8) & 255u) + (int)qy;
             p = ly * T + lx;
             const RasterRec& r = srec[warp][j];
+            float b0, b1, b2;
             covered = cover_test(r.ax, r.ay, r.e1x, r.e1y, r.e2x, r.e2y, r.uz, ((r.view >> kRecFlagShift) & kRecExact) != 0u,
                                  (float)(ox + lx), (float)(oy + ly), b0, b1, b2);
             if (covered) {
+              frags++;
               // interpolate_depth (graphics.cpp:186-194)
               const float z = fa(fa(fa(0.f, fm(r.d2, b2)), fm(r.d1, b1)), fm(r.d0, b0));
               key = ((unsigned long long)ord_bits(z) << 32) | (unsigned long long)(0xfffffffeu - r.seq);
@@ -261,14 +296,7 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
             }
           }
           __syncwarp();
-          if (covered && old > key && st.key[p] == key) {
-            const RasterRec& r = srec[warp][j];
-            st.pay[p] = r.pad;
-            st.seq[p] = r.seq;
-            st.b0[p] = b0;
-            st.b1[p] = b1;
-            st.b2[p] = b2;
-          }
+          if (covered && old > key && st.key[p] == key) st.rec[p] = srec[warp][j].rsv;
           __syncwarp();
         }
       }
@@ -287,7 +315,11 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
         default: shaded = shade_tile<T, HSR_SHADER_FLAT>(v, sc, st, ox, oy, clear, bt); break;
       }
       shaded = __reduce_add_sync(kFull, shaded);
-      if (lane == 0 && shaded) atomicAdd(&sc.ctl->shaded_px, (unsigned long long)shaded);
+      frags = __reduce_add_sync(kFull, frags);
+      if (lane == 0) {
+        if (shaded) atomicAdd(&sc.ctl->shaded_px, (unsigned long long)shaded);
+        if (frags) atomicAdd(&sc.ctl->frag_px, (unsigned long long)frags);
+      }
     }
     if (v.has_dependents) {
       // publish this tile's writes before counting it done (a later view reads them)
@@ -295,7 +327,9 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
       __syncwarp();
       if (lane == 0) atomicAdd(&sc.view_done[vi], 1u);
     }
-    t = __shfl_sync(kFull, t_next, 0);
+    t = t_next;
+    n = n_next;
+    off = off_next;
   }
 }
 

@@ -281,6 +281,7 @@ typedef struct hsr_timing {
   uint64_t vertices;       /* positions transformed                                    */
   uint64_t normals;        /* normals transformed                                      */
   uint64_t clipped_faces;  /* faces that went through the homogeneous clipper          */
+  uint64_t fragments;      /* covered (pixel, triangle) pairs tested against the depth  */
 } hsr_timing;
 HSR_API int hsr_set_profiling(int on);
 HSR_API int hsr_last_timing(hsr_timing* out);

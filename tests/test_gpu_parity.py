@@ -97,6 +97,23 @@ def test_soup_ties_vs_oracle(gpu):
     assert got["main"]["prim"].max() <= frame.mesh.nfaces
 
 
+def test_soup_4m_3840x2160_vs_oracle(gpu):
+    """The full depth-order stress workload: 4M triangles at 3840x2160, lognormal edges
+    (median 2 px), ~8x depth complexity, 1% exact duplicates submitted later."""
+    frame = scenes.soup_frame()
+    assert frame.mesh.nfaces == 4_000_000 and (frame.width, frame.height) == (3840, 2160)
+    got = gpu_render(gpu, frame)
+    assert_parity(got, oracle_expect(frame), "soup4m-2160p")
+    # the equal-depth duplicates win the pixels of their originals wherever those are visible
+    faces = frame.mesh.faces[:, :, 0]
+    _, first = np.unique(faces, axis=0, return_index=True)
+    is_dup = np.ones(len(faces), bool)
+    is_dup[first] = False
+    prim = got["main"]["prim"]
+    owners = prim[prim > 0].astype(np.int64) - 1
+    assert is_dup[owners].sum() > 0
+
+
 def test_multi_draw_same_target(gpu):
     """Two graphics_draw_triangle calls into one RenderBuffer keep the sequential depth test:
     the second draw tests against the first's depth, prim ids offset by prim_base."""
