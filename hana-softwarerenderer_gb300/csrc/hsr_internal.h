@@ -41,7 +41,9 @@ constexpr uint32_t kErrCapacity = kErrRecOverflow | kErrClipOverflow | kErrBinOv
 enum : uint32_t {
   kRecExact = 1u,  // coordinates outside the range where the division-free coverage test is
                    // exact: the raster evaluates the reference's divisions instead
+  kRecHole = 2u,   // slot of a huge triangle handed to k_big: binned nowhere
 };
+constexpr uint32_t kPadPending = 0xffffffffu;  // RasterRec::pad of a record k_emit has not finished
 
 // One triangle that reached the raster (64 bytes).  A, B-A, C-A are the per-triangle
 // constants of barycentric() (graphics.cpp:222-233); uz is u.z, constant per triangle.
@@ -152,7 +154,8 @@ struct Scratch {
 
 // Kernel launchers (kernels_*.cu).  All return cudaError_t as int.
 int launch_vertex(const DView* views, const Chunk* chunks, int nchunks, cudaStream_t s);
-int launch_setup(const DView* views, const Chunk* chunks, int nchunks, int tile, Scratch sc, cudaStream_t s);
+int launch_setup(const DView* views, const Chunk* chunks, int nchunks, Scratch sc, int grid, cudaStream_t s);
+int launch_emit(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s);
 int launch_post(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s);
 int launch_big(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s);
 int launch_scan(Scratch sc, cudaStream_t s);

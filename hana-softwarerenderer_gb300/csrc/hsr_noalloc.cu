@@ -181,14 +181,15 @@ static int noalloc_draw(Runtime* rt, const hsr_draw_desc& d) {
   e = cudaMemsetAsync(dev + o_zero, 0, zero_bytes, s);  // counters start at zero every call
   if (e != cudaSuccess) return cuda_fail(e, "draw_noalloc: clear counters");
   int kr = launch_vertex(dview, (const Chunk*)(dev + o_vch), (int)nvch, s);
-  if (!kr) kr = launch_setup(dview, (const Chunk*)(dev + o_sch), (int)nsch, T, sc, s);
+  if (!kr) kr = launch_setup(dview, (const Chunk*)(dev + o_sch), (int)nsch, sc, rt->num_sms * 4, s);
+  if (!kr) kr = launch_emit(dview, T, sc, rt->num_sms * 8, s);
   if (!kr) kr = launch_post(dview, T, sc, rt->num_sms * 4, s);
   if (!kr) kr = launch_big(dview, T, sc, rt->num_sms * 2, s);
   if (!kr) kr = launch_scan(sc, s);
   if (!kr) kr = launch_scatter(dview, T, sc, (int)std::max<size_t>((rec_cap + 255) / 256, 1), s);
   if (!kr) kr = launch_raster(dview, T, sc, rt->num_sms * rt->tuning.ctas_per_sm, rt->tuning.warps_per_cta, s);
   if (kr) return cuda_fail((cudaError_t)kr, "draw_noalloc: kernel launch");
-  rt->launches += 7;
+  rt->launches += 8;
   Ctl* hc = reinterpret_cast<Ctl*>(h + host_bytes);
   e = cudaMemcpyAsync(hc, sc.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);

@@ -329,8 +329,10 @@ int Plan::enqueue(cudaStream_t s, int num_sms, const hsr_tuning& tu, cudaEvent_t
   int kr = launch_vertex(dviews, (const Chunk*)(dev + o_vch), (int)vchunks.size(), s);
   if (kr) return cuda_fail((cudaError_t)kr, "vertex kernel");
   if (ev && ev[2]) cudaEventRecord(ev[2], s);
-  kr = launch_setup(dviews, (const Chunk*)(dev + o_sch), (int)schunks.size(), tile, sc, s);
+  kr = launch_setup(dviews, (const Chunk*)(dev + o_sch), (int)schunks.size(), sc, num_sms * 4, s);
   if (kr) return cuda_fail((cudaError_t)kr, "setup kernel");
+  kr = launch_emit(dviews, tile, sc, num_sms * 8, s);
+  if (kr) return cuda_fail((cudaError_t)kr, "emit kernel");
   kr = launch_post(dviews, tile, sc, num_sms * 4, s);
   if (kr) return cuda_fail((cudaError_t)kr, "post kernel");
   kr = launch_big(dviews, tile, sc, num_sms * 2, s);
@@ -353,7 +355,7 @@ int Plan::enqueue(cudaStream_t s, int num_sms, const hsr_tuning& tu, cudaEvent_t
 }
 
 int Plan::kernel_count() const {
-  return (vchunks.empty() ? 0 : 1) + (schunks.empty() ? 0 : 1) + 2 + (nscan > 0 ? 1 : 0) + 2;
+  return (vchunks.empty() ? 0 : 1) + (schunks.empty() ? 0 : 1) + 3 + (nscan > 0 ? 1 : 0) + 2;
 }
 
 // Grow the capacity an overflow reported; returns false if nothing overflowed.

@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(256) k_scatter(const DView* __restrict__ views
     const uint32_t i = i0 + (uint32_t)lane;
     const bool ok = i < nrec;
     int tx0 = 0, ty0 = 0, ntw = 0, nt = 0, tbase = 0, tiles_x = 0;
-    if (ok) {
+    if (ok && !((sc.recs[i].view >> kRecFlagShift) & kRecHole)) {  // holes: huge triangles split by k_big
       const RasterRec& r = sc.recs[i];
       const uint32_t xr = r.xr, yr = r.yr;
       const DView& v = views[r.view & kRecViewMask];

@@ -16,6 +16,8 @@
 // Sutherland-Hodgman while every lane evaluates the plane tests on the clip coordinates.
 #include <float.h>
 
+#include <algorithm>
+
 #include "hsr_device.cuh"
 
 namespace hsr {
@@ -299,19 +301,17 @@ __device__ __forceinline__ uint32_t block_reserve(bool want, uint32_t* counter) 
   return want ? s_base + s_count[warp] + (uint32_t)__popc(m & ((1u << lane) - 1u)) : ~0u;
 }
 
-// Store the records of a warp at their reserved slots (at most one per lane, each touching
-// <= kMaxRecordTiles tiles) and count the tiles they touch, aggregating equal tiles across
-// lanes.  All 32 lanes call this.
-__device__ void append_small(bool valid, uint32_t slot, const RasterRec& r, const Payload& pl, int nf4, const DView& v,
-                             int T, const Scratch& sc) {
+// Store the records of a warp at their slots (at most one per lane, each touching
+// <= kMaxRecordTiles tiles) with their payloads, and count the tiles they touch,
+// aggregating equal tiles across lanes.  All 32 lanes call this.
+// With `only_pad`, the record is already in place and only its payload index is written.
+__device__ void append_counts(bool valid, uint32_t slot, const RasterRec& r, const Payload& pl, int nf4, const DView& v,
+                              int T, const Scratch& sc, bool only_pad = false) {
   const int lane = threadIdx.x & 31;
-  const bool ok = valid && slot < sc.rec_cap;
-  if (valid && !ok) atomicOr(&sc.ctl->error, kErrRecOverflow);
   int tx0 = 0, ty0 = 0, ntw = 1, nt = 0;
-  if (ok) {
-    RasterRec w = r;
-    w.pad = slot;  // payload index
-    store_rec(&sc.recs[slot], w);
+  if (valid) {
+    if (only_pad) sc.recs[slot].pad = r.pad;
+    else store_rec(&sc.recs[slot], r);
     store_payload(&sc.pay[slot], pl, nf4);
     rec_tiles(r, T, tx0, ty0, ntw, nt);
   }
@@ -323,6 +323,15 @@ __device__ void append_small(bool valid, uint32_t slot, const RasterRec& r, cons
     if (tile >= 0 && lane == __ffs(grp) - 1) atomicAdd(&sc.tile_count[tile], (uint32_t)__popc(grp));
     if (++kx == ntw) { kx = 0; ky++; }
   }
+}
+
+// append_counts at slots reserved by the caller, checked against the record capacity.
+__device__ void append_small(bool valid, uint32_t slot, RasterRec r, const Payload& pl, int nf4, const DView& v,
+                             int T, const Scratch& sc) {
+  const bool ok = valid && slot < sc.rec_cap;
+  if (valid && !ok) atomicOr(&sc.ctl->error, kErrRecOverflow);
+  r.pad = slot;  // payload index
+  append_counts(ok, slot, r, pl, nf4, v, T, sc);
 }
 
 // True when the reference's clipper returns 0 vertices for this face without creating any
@@ -346,90 +355,171 @@ constexpr int kSetupThreads = 256;
 constexpr int kPolyStride = kVaryings;  // floats per polygon vertex in shared memory
 
 
-__global__ void __launch_bounds__(kSetupThreads, 4) k_setup(const DView* __restrict__ views,
-                                                         const Chunk* __restrict__ chunks, int T, Scratch sc) {
-  const Chunk ch = chunks[blockIdx.x];
-  const DView& v = views[ch.view];
-  const int f = ch.begin + (int)threadIdx.x;
-  const bool active = f < ch.end;
-
-  // ---- fast accept (graphics.cpp:140-148) ---------------------------------------------
-  bool needs_clip = false, valid = false;
-  RasterRec r;
-  Payload pl;
-  if (active) {
-    const int4 iv = __ldg(&v.fv[f]);
-    const int pi[3] = {iv.x, iv.y, iv.z};
-    float4 sv[3];
+// Cull pass, one thread per face: fast accept, cull, viewport, bounding box and the
+// coverage check of small ranges; a surviving triangle's 64-byte record is stored at a
+// block-reserved slot (pad = kPadPending: payload and tile counts are still to come), and
+// faces that need the clipper are queued.  Four in five faces of the serving batches die
+// here, so the per-record work runs in k_emit on dense warps instead of on the few lanes
+// that survive in each warp of this pass.
+//
+// Persistent: block b takes chunks b, b + grid, ... (256 faces each) and loads the face
+// indices of its next chunk while it culls the current one, so the index stream from HBM
+// overlaps the gathers and arithmetic instead of waiting at the head of every chunk.
+__device__ __forceinline__ void cull_face(const DView& v, int f, uint32_t view, int4 iv, bool& valid,
+                                          bool& needs_clip, RasterRec& r) {
+  const int pi[3] = {iv.x, iv.y, iv.z};
+  float4 sv[3];
 #pragma unroll
-    for (int k = 0; k < 3; k++) sv[k] = __ldg(&v.sv[pi[k]]);
-    bool accept = sv_normal(sv[0]) && sv_normal(sv[1]) && sv_normal(sv[2]);
-    if (!accept) {
-      const uint32_t m0 = sv_mask(sv[0]), m1 = sv_mask(sv[1]), m2 = sv_mask(sv[2]);
-      if (m0 & m1 & m2 & 0x80u) {
-        // all three visible, one with w < 1e-5: fast accept, divide here
-        accept = true;
+  for (int k = 0; k < 3; k++) sv[k] = __ldg(&v.sv[pi[k]]);
+  bool accept = sv_normal(sv[0]) && sv_normal(sv[1]) && sv_normal(sv[2]);
+  if (!accept) {
+    const uint32_t m0 = sv_mask(sv[0]), m1 = sv_mask(sv[1]), m2 = sv_mask(sv[2]);
+    if (m0 & m1 & m2 & 0x80u) {
+      // all three visible, one with w < 1e-5: fast accept (graphics.cpp:140-148), divide here
+      accept = true;
 #pragma unroll
-        for (int k = 0; k < 3; k++) {
-          const float4 c = clip_of(v, pi[k]);
-          const F3 n = ndc_of(c);
-          sv[k] = make_float4(n.x, n.y, n.z, fd(1.f, c.w));
-        }
-      } else {
-        needs_clip = !clip_trivially_empty(m0, m1, m2);
+      for (int k = 0; k < 3; k++) {
+        const F3 n = ndc_of(clip_of(v, pi[k]));
+        sv[k] = make_float4(n.x, n.y, n.z, 0.f);
       }
-    }
-    if (accept) {
-      valid = build_rec(v, {sv[0].x, sv[0].y, sv[0].z}, {sv[1].x, sv[1].y, sv[1].z}, {sv[2].x, sv[2].y, sv[2].z},
-                        (uint32_t)f << 4, (uint32_t)ch.view, r);
-      const int nf4 = payload_f4(v.shader);
-      if (valid && nf4 > 0) {
-        // corner varyings of the three vertex() calls (Payload layout)
-        int4 it = iv, in = iv;  // meshes whose v, vt and vn indices agree skip two loads
-        if (!v.unified) {
-          if (v.uv && nf4 >= 3) it = __ldg(&v.fvt[f]);
-          if (v.wnrm) in = __ldg(&v.fvn[f]);
-        }
-        const int ti[3] = {it.x, it.y, it.z}, ni[3] = {in.x, in.y, in.z};
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-          const float4 wp = v.wpos ? __ldg(&v.wpos[pi[k]]) : make_float4(0.f, 0.f, 0.f, 0.f);
-          const float4 wn = v.wnrm ? __ldg(&v.wnrm[ni[k]]) : make_float4(0.f, 0.f, 0.f, 0.f);
-          const float2 t = (v.uv && nf4 >= 3) ? __ldg(&v.uv[ti[k]]) : make_float2(0.f, 0.f);
-          pl.f[k] = sv[k].w;  // recip_w (graphics.cpp:333-337)
-          pl.f[3 + k] = v.shader == HSR_SHADER_SHADOW ? clip_of(v, pi[k]).z : wn.w;
-          pl.f[6 + 2 * k] = t.x;
-          pl.f[7 + 2 * k] = t.y;
-          pl.f[12 + 3 * k] = wn.x; pl.f[13 + 3 * k] = wn.y; pl.f[14 + 3 * k] = wn.z;
-          pl.f[21 + 3 * k] = wp.x; pl.f[22 + 3 * k] = wp.y; pl.f[23 + 3 * k] = wp.z;
-        }
-        pl.f[30] = 0.f;
-        pl.f[31] = 0.f;
-      }
-    }
-  }
-  int tx0, ty0, ntw, nt = 0;
-  if (valid) rec_tiles(r, T, tx0, ty0, ntw, nt);
-  const bool big = valid && nt > kMaxRecordTiles;
-  const uint32_t slot = block_reserve<kSetupThreads>(valid && !big, &sc.ctl->rec_count);
-  append_small(valid && !big, slot, r, pl, payload_f4(v.shader), v, T, sc);
-
-  // huge triangles and faces that need the clipper are queued for k_post, which spreads
-  // them over the whole GPU instead of leaving one warp to work through a cluster of them
-  const uint32_t bslot = warp_reserve(big, &sc.ctl->big_count);
-  if (big) {
-    if (bslot < sc.big_cap) {
-      store_rec(&sc.bigq[bslot].rec, r);
-      store_payload(&sc.bigq[bslot].pay, pl, payload_f4(v.shader));
     } else {
-      atomicOr(&sc.ctl->error, kErrBigOverflow);
+      needs_clip = !clip_trivially_empty(m0, m1, m2);
     }
   }
-  const uint32_t cslot = warp_reserve(needs_clip, &sc.ctl->clip_count);
-  if (needs_clip) {
-    if (cslot < sc.clip_cap) sc.clipq[cslot] = make_int2(ch.view, f);
-    else atomicOr(&sc.ctl->error, kErrClipOverflow);
+  if (accept)
+    valid = build_rec(v, {sv[0].x, sv[0].y, sv[0].z}, {sv[1].x, sv[1].y, sv[1].z}, {sv[2].x, sv[2].y, sv[2].z},
+                      (uint32_t)f << 4, view, r);
+}
+
+__global__ void __launch_bounds__(kSetupThreads, 4) k_setup(const DView* __restrict__ views,
+                                                         const Chunk* __restrict__ chunks, int nchunks, Scratch sc) {
+  int c = (int)blockIdx.x;
+  const int c_end = nchunks;
+  if (c >= c_end) return;
+  Chunk ch = chunks[c];
+  int4 iv = make_int4(0, 0, 0, 0);
+  if (ch.begin + (int)threadIdx.x < ch.end) iv = __ldg(&views[ch.view].fv[ch.begin + (int)threadIdx.x]);
+  for (;;) {
+    // the next chunk's face indices: issued now, consumed next iteration
+    const bool more = c + (int)gridDim.x < c_end;
+    Chunk chn = ch;
+    int4 ivn = make_int4(0, 0, 0, 0);
+    if (more) {
+      chn = chunks[c + (int)gridDim.x];
+      if (chn.begin + (int)threadIdx.x < chn.end) ivn = __ldg(&views[chn.view].fv[chn.begin + (int)threadIdx.x]);
+    }
+    const DView& v = views[ch.view];
+    const int f = ch.begin + (int)threadIdx.x;
+    bool needs_clip = false, valid = false;
+    RasterRec r;
+    if (f < ch.end) cull_face(v, f, (uint32_t)ch.view, iv, valid, needs_clip, r);
+    const uint32_t slot = block_reserve<kSetupThreads>(valid, &sc.ctl->rec_count);
+    if (valid) {
+      if (slot < sc.rec_cap) {
+        r.pad = kPadPending;
+        store_rec(&sc.recs[slot], r);
+      } else {
+        atomicOr(&sc.ctl->error, kErrRecOverflow);
+      }
+    }
+    const uint32_t cslot = warp_reserve(needs_clip, &sc.ctl->clip_count);
+    if (needs_clip) {
+      if (cslot < sc.clip_cap) sc.clipq[cslot] = make_int2(ch.view, f);
+      else atomicOr(&sc.ctl->error, kErrClipOverflow);
+    }
+    if (!more) break;
+    c += (int)gridDim.x;
+    ch = chn;
+    iv = ivn;
   }
+}
+
+// Payload of an unclipped face from the vertex stage's outputs (Payload layout): the corner
+// varyings of its three vertex() calls and their 1/w.
+__device__ __forceinline__ void face_payload(const DView& v, int f, int nf4, Payload& pl) {
+  const int4 iv = __ldg(&v.fv[f]);
+  int4 it = iv, in = iv;  // meshes whose v, vt and vn indices agree skip two loads
+  if (!v.unified) {
+    if (v.uv && nf4 >= 3) it = __ldg(&v.fvt[f]);
+    if (v.wnrm) in = __ldg(&v.fvn[f]);
+  }
+  const int pi[3] = {iv.x, iv.y, iv.z}, ti[3] = {it.x, it.y, it.z}, ni[3] = {in.x, in.y, in.z};
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const float4 s = __ldg(&v.sv[pi[k]]);
+    const float4 wp = v.wpos ? __ldg(&v.wpos[pi[k]]) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 wn = v.wnrm ? __ldg(&v.wnrm[ni[k]]) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2 t = (v.uv && nf4 >= 3) ? __ldg(&v.uv[ti[k]]) : make_float2(0.f, 0.f);
+    // recip_w (graphics.cpp:333-337): from the screen vertex, or divided here for a visible
+    // vertex with w < 1e-5 (the only kind of special vertex a fast-accepted face can have)
+    float rw = s.w;
+    float4 c;
+    const bool special = !sv_normal(s);
+    if (special || v.shader == HSR_SHADER_SHADOW) c = clip_of(v, pi[k]);
+    if (special) rw = fd(1.f, c.w);
+    pl.f[k] = rw;
+    pl.f[3 + k] = v.shader == HSR_SHADER_SHADOW ? c.z : wn.w;
+    pl.f[6 + 2 * k] = t.x;
+    pl.f[7 + 2 * k] = t.y;
+    pl.f[12 + 3 * k] = wn.x; pl.f[13 + 3 * k] = wn.y; pl.f[14 + 3 * k] = wn.z;
+    pl.f[21 + 3 * k] = wp.x; pl.f[22 + 3 * k] = wp.y; pl.f[23 + 3 * k] = wp.z;
+  }
+  pl.f[30] = 0.f;
+  pl.f[31] = 0.f;
+}
+
+// Emit pass over the records of k_setup (dense: one thread per surviving triangle): the
+// shading payload, the tile counts, and the hand-over of huge triangles to k_big (their
+// slot becomes a hole the binning skips).  Grid-stride with warp-uniform trip counts, so
+// the warp collectives of append_small see every lane.
+__global__ void __launch_bounds__(kSetupThreads) k_emit(const DView* __restrict__ views, int T, Scratch sc) {
+  const int lane = threadIdx.x & 31;
+  if (sc.ctl->error & kErrCapacity) return;
+  const uint32_t nrec = min(sc.ctl->rec_count, sc.rec_cap);
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < nrec; i0 += stride) {
+    const uint32_t i = i0 + (uint32_t)lane;
+    bool valid = false;
+    RasterRec r;
+    Payload pl;
+    int nf4 = 0;
+    const DView* v = views;
+    if (i < nrec) {
+      // the words this pass needs (seq, view, pixel range, pad); the whole record only
+      // for a huge triangle
+      const uint4 a = *reinterpret_cast<const uint4*>(reinterpret_cast<const char*>(&sc.recs[i]) + 32);
+      const uint4 b = *reinterpret_cast<const uint4*>(reinterpret_cast<const char*>(&sc.recs[i]) + 48);
+      r.seq = a.z; r.view = a.w; r.xr = b.x; r.yr = b.y; r.rsv = b.z; r.pad = b.w;
+      valid = r.pad == kPadPending;  // written by k_setup in this launch sequence
+      if (valid) {
+        v = views + (r.view & kRecViewMask);
+        nf4 = payload_f4(v->shader);
+        if (nf4 > 0) face_payload(*v, (int)(r.seq >> 4), nf4, pl);
+      }
+    }
+    int tx0, ty0, ntw, nt = 0;
+    if (valid) rec_tiles(r, T, tx0, ty0, ntw, nt);
+    const bool big = valid && nt > kMaxRecordTiles;
+    const bool small = valid && !big;
+    if (small) r.pad = i;  // payload index
+    append_counts(small, i, r, pl, nf4, *v, T, sc, true);
+    const uint32_t bslot = warp_reserve(big, &sc.ctl->big_count);
+    if (big) {
+      r = sc.recs[i];
+      sc.recs[i].view = r.view | (kRecHole << kRecFlagShift);
+      if (bslot < sc.big_cap) {
+        store_rec(&sc.bigq[bslot].rec, r);
+        store_payload(&sc.bigq[bslot].pay, pl, nf4);
+      } else {
+        atomicOr(&sc.ctl->error, kErrBigOverflow);
+      }
+    }
+  }
+}
+
+int launch_emit(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s) {
+  k_emit<<<grid, kSetupThreads, 0, s>>>(views, tile, sc);
+  return (int)cudaGetLastError();
 }
 
 // Homogeneous clipping of one face by one warp (graphics.cpp:73-161): lane k carries
@@ -456,10 +546,12 @@ __device__ void clip_face(const DView& v, int view, int face, int T, const Scrat
   int n = 3;
   float* src = A;
   float* dst = B;
-  for (int plane = PW; plane <= NZ && n >= 3; plane++) {
+#pragma unroll
+  for (int plane = PW; plane <= NZ; plane++) {
+    if (n < 3) break;
     int m = 0;
     for (int i = 0; i < n; i++) {
-      const float* prev = src + ((i - 1 + n) % n) * kPolyStride;
+      const float* prev = src + (i == 0 ? n - 1 : i - 1) * kPolyStride;
       const float* curr = src + i * kPolyStride;
       const bool pin = inside_plane(prev, plane), cin = inside_plane(curr, plane);
       if (pin != cin) {
@@ -591,9 +683,9 @@ int launch_big(const DView* views, int tile, Scratch sc, int grid, cudaStream_t 
   return (int)cudaGetLastError();
 }
 
-int launch_setup(const DView* views, const Chunk* chunks, int nchunks, int tile, Scratch sc, cudaStream_t s) {
+int launch_setup(const DView* views, const Chunk* chunks, int nchunks, Scratch sc, int grid, cudaStream_t s) {
   if (nchunks <= 0) return 0;
-  k_setup<<<nchunks, kSetupThreads, 0, s>>>(views, chunks, tile, sc);
+  k_setup<<<std::max(1, std::min(grid, nchunks)), kSetupThreads, 0, s>>>(views, chunks, nchunks, sc);
   return (int)cudaGetLastError();
 }
 
