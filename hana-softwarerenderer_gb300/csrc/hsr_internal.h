@@ -104,7 +104,14 @@ struct __align__(128) DView {
   const uint32_t* normal;  int32_t nw, nh, nbpp;
   // shadow map (colour plane of another target), null when ShaderData::shadow_map is null
   const uint32_t* sm_color; int32_t smW, smH;
+  // this view's work chunks in the batch's chunk spaces (a kernel finds the view of chunk c
+  // as the last view whose base is <= c): vertex chunks of kVertexChunk items (its position
+  // chunks, then its normal chunks), setup chunks of kSetupChunk faces
+  int32_t vch_base, vch_npos, vch_count;
+  int32_t sch_base;
 };
+constexpr int kVertexChunk = 1024;  // positions or normals per vertex-stage chunk
+constexpr int kSetupChunk = 256;    // faces per setup chunk (one per thread of a block)
 static_assert(offsetof(DView, prim_base) + sizeof(uint32_t) <= 128, "per-tile fields must share one line");
 
 struct Ctl {
@@ -134,6 +141,7 @@ struct Chunk {
   int32_t begin;
   int32_t end;
 };
+constexpr int kSharedViews = 256;  // views whose chunk / tile bases kernels copy to shared memory
 
 // Scratch of one launch sequence (device pointers, sized by the host).
 struct Scratch {
@@ -153,8 +161,8 @@ struct Scratch {
 };
 
 // Kernel launchers (kernels_*.cu).  All return cudaError_t as int.
-int launch_vertex(const DView* views, const Chunk* chunks, int nchunks, cudaStream_t s);
-int launch_setup(const DView* views, const Chunk* chunks, int nchunks, Scratch sc, int grid, cudaStream_t s);
+int launch_vertex(const DView* views, int nviews, int nchunks, int grid, cudaStream_t s);
+int launch_setup(const DView* views, int nviews, int nchunks, Scratch sc, int grid, cudaStream_t s);
 int launch_emit(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s);
 int launch_post(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s);
 int launch_big(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s);

@@ -35,14 +35,15 @@
 namespace hsr {
 
 constexpr size_t kStaticScratchBytes = size_t(128) << 20;
-constexpr size_t kStaticHostBytes = size_t(1) << 20;
+constexpr size_t kStaticHostBytes = 4096;
 constexpr int kMaxDevices = 64;
 
 // The scratch every call uses.  In host code this name is only a host-side stand-in for
 // the device array: its device address comes from cudaGetSymbolAddress, per device.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kStaticScratchBytes];
 
-static unsigned char g_noalloc_host[kStaticHostBytes];  // view descriptor, chunks, control block
+static unsigned char g_noalloc_host[kStaticHostBytes];  // view descriptor and control block
+static_assert(((sizeof(DView) + 255) / 256 * 256) + sizeof(Ctl) <= kStaticHostBytes, "host staging too small");
 static void* g_noalloc_dev[kMaxDevices];
 
 static size_t nal(size_t x) { return (x + 255) / 256 * 256; }
@@ -110,16 +111,18 @@ static int noalloc_draw(Runtime* rt, const hsr_draw_desc& d) {
 
   // ---- work chunks and the fixed layout of the static array ------------------------------
   const bool wnrm = needs_wnrm_h(d.shader);
-  const size_t nvch = (size_t)(m->npos + 1023) / 1024 + (wnrm ? (size_t)(m->nnrm + 1023) / 1024 : 0);
-  const size_t nsch = (size_t)(m->nfaces + 255) / 256;
+  v.vch_base = 0;
+  v.vch_npos = (m->npos + kVertexChunk - 1) / kVertexChunk;
+  v.vch_count = v.vch_npos + (wnrm ? (m->nnrm + kVertexChunk - 1) / kVertexChunk : 0);
+  v.sch_base = 0;
+  const int nvch = v.vch_count;
+  const int nsch = (m->nfaces + kSetupChunk - 1) / kSetupChunk;
   const size_t faces = (size_t)m->nfaces, tiles = (size_t)v.ntiles;
   const size_t rec_cap = faces + faces / 4 + 1024, clip_cap = faces / 16 + 256, big_cap = faces / 64 + 256;
   const size_t bin_cap = (size_t)(rt->tuning.bin_factor * (double)(faces + tiles)) + 4096;
   const int nscan = scan_blocks((int)tiles);
   size_t off = 0;
   const size_t o_view = off; off = nal(off + sizeof(DView));
-  const size_t o_vch = off; off = nal(off + sizeof(Chunk) * std::max<size_t>(nvch, 1));
-  const size_t o_sch = off; off = nal(off + sizeof(Chunk) * std::max<size_t>(nsch, 1));
   const size_t host_bytes = off;
   const size_t o_clip = off; off = nal(off + sizeof(float4) * (size_t)std::max(m->npos, 1));
   const size_t o_wpos = off; if (needs_wpos_h(d.shader)) off = nal(off + sizeof(float4) * (size_t)std::max(m->npos, 1));
@@ -139,8 +142,6 @@ static int noalloc_draw(Runtime* rt, const hsr_draw_desc& d) {
   const size_t o_bins = off; off = nal(off + sizeof(uint32_t) * bin_cap);
   if (off > kStaticScratchBytes)
     return fail(HSR_ERR_INVALID_ARG, "draw_noalloc: the draw needs more scratch than the 128 MiB the allocation-free path holds");
-  if (host_bytes + sizeof(Ctl) > kStaticHostBytes)
-    return fail(HSR_ERR_INVALID_ARG, "draw_noalloc: too many work chunks for the static staging array");
 
   v.sv = (float4*)(dev + o_clip);
   v.wpos = needs_wpos_h(d.shader) ? (float4*)(dev + o_wpos) : nullptr;
@@ -148,14 +149,6 @@ static int noalloc_draw(Runtime* rt, const hsr_draw_desc& d) {
 
   unsigned char* h = g_noalloc_host;
   std::memcpy(h + o_view, &v, sizeof(DView));
-  Chunk* vch = reinterpret_cast<Chunk*>(h + o_vch);
-  size_t k = 0;
-  for (int b = 0; b < m->npos; b += 1024) vch[k++] = {0, 0, b, std::min(m->npos, b + 1024)};
-  if (wnrm)
-    for (int b = 0; b < m->nnrm; b += 1024) vch[k++] = {0, 1, b, std::min(m->nnrm, b + 1024)};
-  Chunk* sch = reinterpret_cast<Chunk*>(h + o_sch);
-  k = 0;
-  for (int b = 0; b < m->nfaces; b += 256) sch[k++] = {0, 0, b, std::min(m->nfaces, b + 256)};
 
   Scratch sc;
   std::memset(&sc, 0, sizeof(sc));
@@ -180,8 +173,8 @@ static int noalloc_draw(Runtime* rt, const hsr_draw_desc& d) {
   if (e != cudaSuccess) return cuda_fail(e, "draw_noalloc: upload");
   e = cudaMemsetAsync(dev + o_zero, 0, zero_bytes, s);  // counters start at zero every call
   if (e != cudaSuccess) return cuda_fail(e, "draw_noalloc: clear counters");
-  int kr = launch_vertex(dview, (const Chunk*)(dev + o_vch), (int)nvch, s);
-  if (!kr) kr = launch_setup(dview, (const Chunk*)(dev + o_sch), (int)nsch, sc, rt->num_sms * 4, s);
+  int kr = launch_vertex(dview, 1, nvch, rt->num_sms * 8, s);
+  if (!kr) kr = launch_setup(dview, 1, nsch, sc, rt->num_sms * 4, s);
   if (!kr) kr = launch_emit(dview, T, sc, rt->num_sms * 8, s);
   if (!kr) kr = launch_post(dview, T, sc, rt->num_sms * 4, s);
   if (!kr) kr = launch_big(dview, T, sc, rt->num_sms * 2, s);

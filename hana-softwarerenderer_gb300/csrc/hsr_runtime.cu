@@ -239,10 +239,12 @@ int Runtime::plan_build(const hsr_draw_desc* descs, int n, Plan& p) {
       bytes = align_up(bytes + sizeof(float4) * (size_t)std::max(m->nnrm, 1), 256);
       p.total_nrm += (size_t)m->nnrm;
     }
-    for (int b = 0; b < m->npos; b += 1024) p.vchunks.push_back({k, 0, b, std::min(m->npos, b + 1024)});
-    if (shader_needs_wnrm(d.shader))
-      for (int b = 0; b < m->nnrm; b += 1024) p.vchunks.push_back({k, 1, b, std::min(m->nnrm, b + 1024)});
-    for (int b = 0; b < m->nfaces; b += 256) p.schunks.push_back({k, 0, b, std::min(m->nfaces, b + 256)});
+    v.vch_base = p.nvch;
+    v.vch_npos = (m->npos + kVertexChunk - 1) / kVertexChunk;
+    v.vch_count = v.vch_npos + (shader_needs_wnrm(d.shader) ? (m->nnrm + kVertexChunk - 1) / kVertexChunk : 0);
+    v.sch_base = p.nsch;
+    p.nvch += v.vch_count;
+    p.nsch += (m->nfaces + kSetupChunk - 1) / kSetupChunk;
   }
   for (int k = 0; k < n; k++) {
     if (p.views[k].dep0 >= 0) p.views[p.views[k].dep0].has_dependents = 1;
@@ -268,8 +270,6 @@ void Plan::layout() {
   //  scan_status | tile_off | recs | clipbuf | bins]; the zeroed part is one memset
   size_t off = 0;
   o_views = off; off = align_up(off + sizeof(DView) * n, 256);
-  o_vch = off; off = align_up(off + sizeof(Chunk) * std::max<size_t>(vchunks.size(), 1), 256);
-  o_sch = off; off = align_up(off + sizeof(Chunk) * std::max<size_t>(schunks.size(), 1), 256);
   host_bytes = off;
   o_vout = off; off = align_up(off + view_bytes, 256);
   o_zero = off;
@@ -299,8 +299,6 @@ void Plan::bind(char* dev_base, char* host_base) {
     v.wnrm = shader_needs_wnrm(v.shader) ? (float4*)(dev + o_vout + offs[k].wnrm) : nullptr;
   }
   std::memcpy(host + o_views, views.data(), sizeof(DView) * n);
-  if (!vchunks.empty()) std::memcpy(host + o_vch, vchunks.data(), sizeof(Chunk) * vchunks.size());
-  if (!schunks.empty()) std::memcpy(host + o_sch, schunks.data(), sizeof(Chunk) * schunks.size());
   sc.ctl = (Ctl*)(dev + o_ctl);
   sc.view_done = (uint32_t*)(dev + o_done);
   sc.recs = (RasterRec*)(dev + o_recs); sc.rec_cap = (uint32_t)rec_cap;
@@ -326,10 +324,10 @@ int Plan::enqueue(cudaStream_t s, int num_sms, const hsr_tuning& tu, cudaEvent_t
   e = cudaMemsetAsync(dev + o_zero, 0, zero_bytes, s);
   if (e != cudaSuccess) return cuda_fail(e, "clear scratch");
   if (ev && ev[1]) cudaEventRecord(ev[1], s);
-  int kr = launch_vertex(dviews, (const Chunk*)(dev + o_vch), (int)vchunks.size(), s);
+  int kr = launch_vertex(dviews, n, nvch, num_sms * 8, s);
   if (kr) return cuda_fail((cudaError_t)kr, "vertex kernel");
   if (ev && ev[2]) cudaEventRecord(ev[2], s);
-  kr = launch_setup(dviews, (const Chunk*)(dev + o_sch), (int)schunks.size(), sc, num_sms * 4, s);
+  kr = launch_setup(dviews, n, nsch, sc, num_sms * 4, s);
   if (kr) return cuda_fail((cudaError_t)kr, "setup kernel");
   kr = launch_emit(dviews, tile, sc, num_sms * 8, s);
   if (kr) return cuda_fail((cudaError_t)kr, "emit kernel");
@@ -355,7 +353,7 @@ int Plan::enqueue(cudaStream_t s, int num_sms, const hsr_tuning& tu, cudaEvent_t
 }
 
 int Plan::kernel_count() const {
-  return (vchunks.empty() ? 0 : 1) + (schunks.empty() ? 0 : 1) + 3 + (nscan > 0 ? 1 : 0) + 2;
+  return (nvch ? 1 : 0) + (nsch ? 1 : 0) + 3 + (nscan > 0 ? 1 : 0) + 2;
 }
 
 // Grow the capacity an overflow reported; returns false if nothing overflowed.

@@ -85,11 +85,72 @@ __device__ __forceinline__ bool sv_normal(float4 s) { return !(fabsf(s.x) > 1.f)
 __device__ __forceinline__ uint32_t sv_mask(float4 s) { return sv_normal(s) ? 0xffu : __float_as_uint(s.y); }
 
 // ---------------------------------------------------------------------------------------
+// work chunks
+// ---------------------------------------------------------------------------------------
+// The chunk bases of all views in shared memory (nviews <= kSharedViews), read with
+// `base_of` (field selector); every thread of the block calls this (ends with a barrier).
+template <class F>
+__device__ __forceinline__ const int32_t* share_bases(const DView* views, int nviews, int32_t* s_base, F base_of) {
+  if (nviews > kSharedViews) return nullptr;
+  for (int i = threadIdx.x; i < nviews; i += blockDim.x) s_base[i] = base_of(views[i]);
+  __syncthreads();
+  return s_base;
+}
+// View of chunk c: the last view whose base is <= c (views with no chunks share the next
+// view's base and are never returned for a chunk they do not hold).  A block visits its
+// chunks in increasing order, so the search walks forward from the view of its previous
+// chunk (`hint`), usually zero or one step.
+template <class F>
+__device__ __forceinline__ int chunk_view(const DView* views, const int32_t* s_base, int nviews, int c, F base_of,
+                                          int hint) {
+  int k = hint;
+  while (k + 1 < nviews && (s_base ? s_base[k + 1] : base_of(views[k + 1])) <= c) k++;
+  return k;
+}
+// The same by binary search, for a block that starts cold.
+template <class F>
+__device__ __forceinline__ int chunk_view_search(const DView* views, const int32_t* s_base, int nviews, int c,
+                                                 F base_of) {
+  int lo = 0, hi = nviews - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if ((s_base ? s_base[mid] : base_of(views[mid])) <= c) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+struct VchBase { __device__ int32_t operator()(const DView& v) const { return v.vch_base; } };
+struct SchBase { __device__ int32_t operator()(const DView& v) const { return v.sch_base; } };
+
+// Chunk c of the vertex stage: view, kind (0 positions, 1 normals) and item range.
+__device__ __forceinline__ Chunk vertex_chunk(const DView* views, const int32_t* s_base, int nviews, int c) {
+  const int k = chunk_view_search(views, s_base, nviews, c, VchBase());
+  const DView& v = views[k];
+  int local = c - v.vch_base;
+  Chunk ch;
+  ch.view = k;
+  ch.kind = local < v.vch_npos ? 0 : 1;
+  if (ch.kind) local -= v.vch_npos;
+  ch.begin = local * kVertexChunk;
+  ch.end = min(ch.kind ? v.nnrm : v.npos, ch.begin + kVertexChunk);
+  return ch;
+}
+// Chunk c of the setup stage: view and face range.
+__device__ __forceinline__ Chunk setup_chunk(const DView* views, const int32_t* s_base, int nviews, int c, int hint) {
+  const int k = chunk_view(views, s_base, nviews, c, SchBase(), hint);
+  const DView& v = views[k];
+  Chunk ch;
+  ch.view = k;
+  ch.kind = 0;
+  ch.begin = (c - v.sch_base) * kSetupChunk;
+  ch.end = min(v.nfaces, ch.begin + kSetupChunk);
+  return ch;
+}
+
+// ---------------------------------------------------------------------------------------
 // vertex stage
 // ---------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_vertex(const DView* __restrict__ views, const Chunk* __restrict__ chunks) {
-  const Chunk ch = chunks[blockIdx.x];
-  const DView& v = views[ch.view];
+// One vertex chunk (kVertexChunk items, 4 per thread).
+__device__ __forceinline__ void vertex_chunk_work(const DView& v, const Chunk& ch) {
   const int i4 = ch.begin + (int)threadIdx.x * 4;
   if (i4 >= ch.end) return;
   if (ch.kind == 0) {
@@ -128,9 +189,18 @@ __global__ void __launch_bounds__(256) k_vertex(const DView* __restrict__ views,
   }
 }
 
-int launch_vertex(const DView* views, const Chunk* chunks, int nchunks, cudaStream_t s) {
+// One block per chunk (the blocks are short and many: their prologues overlap others' work).
+__global__ void __launch_bounds__(256) k_vertex(const DView* __restrict__ views, int nviews) {
+  __shared__ int32_t s_base[kSharedViews];
+  const int32_t* base = share_bases(views, nviews, s_base, VchBase());
+  const Chunk ch = vertex_chunk(views, base, nviews, (int)blockIdx.x);
+  vertex_chunk_work(views[ch.view], ch);
+}
+
+int launch_vertex(const DView* views, int nviews, int nchunks, int grid, cudaStream_t s) {
+  (void)grid;
   if (nchunks <= 0) return 0;
-  k_vertex<<<nchunks, 256, 0, s>>>(views, chunks);
+  k_vertex<<<nchunks, 256, 0, s>>>(views, nviews);
   return (int)cudaGetLastError();
 }
 
@@ -391,12 +461,14 @@ __device__ __forceinline__ void cull_face(const DView& v, int f, uint32_t view, 
                       (uint32_t)f << 4, view, r);
 }
 
-__global__ void __launch_bounds__(kSetupThreads, 4) k_setup(const DView* __restrict__ views,
-                                                         const Chunk* __restrict__ chunks, int nchunks, Scratch sc) {
+__global__ void __launch_bounds__(kSetupThreads, 4) k_setup(const DView* __restrict__ views, int nviews,
+                                                         int nchunks, Scratch sc) {
+  __shared__ int32_t s_base[kSharedViews];
+  const int32_t* base = share_bases(views, nviews, s_base, SchBase());
   int c = (int)blockIdx.x;
   const int c_end = nchunks;
   if (c >= c_end) return;
-  Chunk ch = chunks[c];
+  Chunk ch = setup_chunk(views, base, nviews, c, 0);
   int4 iv = make_int4(0, 0, 0, 0);
   if (ch.begin + (int)threadIdx.x < ch.end) iv = __ldg(&views[ch.view].fv[ch.begin + (int)threadIdx.x]);
   for (;;) {
@@ -405,7 +477,7 @@ __global__ void __launch_bounds__(kSetupThreads, 4) k_setup(const DView* __restr
     Chunk chn = ch;
     int4 ivn = make_int4(0, 0, 0, 0);
     if (more) {
-      chn = chunks[c + (int)gridDim.x];
+      chn = setup_chunk(views, base, nviews, c + (int)gridDim.x, ch.view);
       if (chn.begin + (int)threadIdx.x < chn.end) ivn = __ldg(&views[chn.view].fv[chn.begin + (int)threadIdx.x]);
     }
     const DView& v = views[ch.view];
@@ -683,9 +755,9 @@ int launch_big(const DView* views, int tile, Scratch sc, int grid, cudaStream_t 
   return (int)cudaGetLastError();
 }
 
-int launch_setup(const DView* views, const Chunk* chunks, int nchunks, Scratch sc, int grid, cudaStream_t s) {
+int launch_setup(const DView* views, int nviews, int nchunks, Scratch sc, int grid, cudaStream_t s) {
   if (nchunks <= 0) return 0;
-  k_setup<<<std::max(1, std::min(grid, nchunks)), kSetupThreads, 0, s>>>(views, chunks, nchunks, sc);
+  k_setup<<<std::max(1, std::min(grid, nchunks)), kSetupThreads, 0, s>>>(views, nviews, nchunks, sc);
   return (int)cudaGetLastError();
 }
 

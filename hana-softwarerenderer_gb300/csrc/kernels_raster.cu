@@ -30,8 +30,6 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr long kWaitLimit = 1L << 23;  // ~1-2 s of polling before a dependency wait gives up
 constexpr uint32_t kNone = 0xffffffffu;
 
-constexpr int kSharedViews = 256;  // views whose first tile index the raster keeps in shared memory
-
 // View owning tile t: the last view whose first tile is <= t (views hold consecutive tile
 // ranges in batch order).  `tbase` is the shared copy when the batch has at most
 // kSharedViews views, else null and the descriptors are searched in global memory.
