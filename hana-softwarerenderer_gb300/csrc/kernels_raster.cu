@@ -77,6 +77,18 @@ __constant__ uint32_t kDivMagic[33] = {0,     65536, 32768, 21846, 16384, 13108,
                                        5958,  5462,  5042,  4682,  4370,  4096,  3856,  3641, 3450, 3277, 3121,
                                        2979,  2850,  2731,  2622,  2521,  2428,  2341,  2260, 2185, 2115, 2048};
 
+// The non-empty records of one batch of a tile list, compacted, one array per field: lanes
+// that read different records then hit different shared-memory banks (a 64-byte record per
+// slot would put every even record's field in one bank).
+struct BatchRecs {
+  float ax[32], ay[32], e1x[32], e1y[32], e2x[32], e2y[32], uz[32], d0[32], d1[32], d2[32];
+  uint32_t seq[32];    // submission order
+  uint32_t idx[32];    // record index
+  uint32_t off[32];    // first candidate of the record's run
+  uint32_t box[32];    // box in the tile: x0 | y0 << 8 | width << 16, bit 31 = kRecExact
+  uint32_t magic[32];  // ceil(65536 / width): row of a candidate by multiply-shift
+};
+
 // Per-warp tile state in shared memory: per pixel the key (ordered depth | submission) and
 // the index of the record that holds it.
 template <int NPIX>
@@ -146,9 +158,7 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
   constexpr int NPIX = T * T;
   constexpr int PPL = NPIX / 32;
   __shared__ TileState<NPIX> sst[WARPS];
-  __shared__ RasterRec srec[WARPS][32];  // the batch's non-empty records, compacted (rsv = index)
-  __shared__ uint32_t soff[WARPS][32];   // first candidate of each
-  __shared__ uint32_t sbox[WARPS][32];   // box in the tile: x0 | y0 << 8 | width << 16
+  __shared__ BatchRecs sbr[WARPS];
   __shared__ float s_u8f[256], s_u8n[256];
   __shared__ int32_t s_tbase[kSharedViews];
   build_byte_tables(s_u8f, s_u8n);
@@ -159,6 +169,7 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
   const ByteTables bt{s_u8f, s_u8n};
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   TileState<NPIX>& st = sst[warp];
+  BatchRecs& br = sbr[warp];
   if (sc.ctl->error & kErrCapacity) return;
   const uint32_t nrec = min(sc.ctl->rec_count, sc.rec_cap);
 
@@ -256,10 +267,14 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
         __syncwarp();
         if (c > 0u) {  // compact the non-empty runs
           const int k = __popc(ne & ((1u << lane) - 1u));
-          rr.rsv = ri;
-          srec[warp][k] = rr;
-          soff[warp][k] = start;
-          sbox[warp][k] = box;
+          br.ax[k] = rr.ax; br.ay[k] = rr.ay; br.e1x[k] = rr.e1x; br.e1y[k] = rr.e1y;
+          br.e2x[k] = rr.e2x; br.e2y[k] = rr.e2y; br.uz[k] = rr.uz;
+          br.d0[k] = rr.d0; br.d1[k] = rr.d1; br.d2[k] = rr.d2;
+          br.seq[k] = rr.seq;
+          br.idx[k] = ri;
+          br.off[k] = start;
+          br.box[k] = box | (((rr.view >> kRecFlagShift) & kRecExact) ? 0x80000000u : 0u);
+          br.magic[k] = kDivMagic[box >> 16];
         }
         __syncwarp();
         for (uint32_t base = 0; base < W; base += 32) {
@@ -274,27 +289,26 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
           if (i < W) {
             // owner: the last run starting at or before candidate i
             j = (int)(before + (uint32_t)__popc(here & ((2u << lane) - 1u))) - 1;
-            const uint32_t q = i - soff[warp][j];
-            const uint32_t bx = sbox[warp][j];
-            const uint32_t lw = bx >> 16;
-            const uint32_t qy = (q * kDivMagic[lw]) >> 16;
+            const uint32_t q = i - br.off[j];
+            const uint32_t bx = br.box[j];
+            const uint32_t lw = (bx >> 16) & 255u;
+            const uint32_t qy = (q * br.magic[j]) >> 16;
             const int lx = (int)(bx & 255u) + (int)(q - qy * lw);
             const int ly = (int)((bx >> 8) & 255u) + (int)qy;
             p = ly * T + lx;
-            const RasterRec& r = srec[warp][j];
             float b0, b1, b2;
-            covered = cover_test(r.ax, r.ay, r.e1x, r.e1y, r.e2x, r.e2y, r.uz, ((r.view >> kRecFlagShift) & kRecExact) != 0u,
-                                 (float)(ox + lx), (float)(oy + ly), b0, b1, b2);
+            covered = cover_test(br.ax[j], br.ay[j], br.e1x[j], br.e1y[j], br.e2x[j], br.e2y[j], br.uz[j],
+                                 (bx >> 31) != 0u, (float)(ox + lx), (float)(oy + ly), b0, b1, b2);
             if (covered) {
               frags++;
               // interpolate_depth (graphics.cpp:186-194)
-              const float z = fa(fa(fa(0.f, fm(r.d2, b2)), fm(r.d1, b1)), fm(r.d0, b0));
-              key = ((unsigned long long)ord_bits(z) << 32) | (unsigned long long)(0xfffffffeu - r.seq);
+              const float z = fa(fa(fa(0.f, fm(br.d2[j], b2)), fm(br.d1[j], b1)), fm(br.d0[j], b0));
+              key = ((unsigned long long)ord_bits(z) << 32) | (unsigned long long)(0xfffffffeu - br.seq[j]);
               old = atomicMin(&st.key[p], key);
             }
           }
           __syncwarp();
-          if (covered && old > key && st.key[p] == key) st.rec[p] = srec[warp][j].rsv;
+          if (covered && old > key && st.key[p] == key) st.rec[p] = br.idx[j];
           __syncwarp();
         }
       }
