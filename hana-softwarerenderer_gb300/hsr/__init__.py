@@ -137,6 +137,15 @@ def lib():
                             ctypes.c_int),
         "hsr_server_now_ms": ([ctypes.c_uint64, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
         "hsr_server_destroy": ([ctypes.c_uint64], ctypes.c_int),
+        "hsr_obj_read": ([ctypes.c_char_p, ctypes.c_uint32, _f32p, _i32p, _f32p, _i32p, _f32p, _i32p, _i32p, _i32p],
+                         ctypes.c_int),
+        "hsr_tga_read": ([ctypes.c_char_p, ctypes.c_uint32, _u8p, _i32p, _i32p, _i32p], ctypes.c_int),
+        "hsr_tga_write": ([ctypes.c_char_p, _u8p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32],
+                          ctypes.c_int),
+        "hsr_mesh_load_obj": ([ctypes.c_char_p, ctypes.c_uint32, _u64p], ctypes.c_int),
+        "hsr_texture_load_tga": ([ctypes.c_char_p, ctypes.c_uint32, _u64p], ctypes.c_int),
+        "hsr_target_present": ([ctypes.c_uint64, _u8p, ctypes.c_int32], ctypes.c_int),
+        "hsr_target_write_tga": ([ctypes.c_uint64, ctypes.c_char_p, ctypes.c_int32], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -227,8 +236,64 @@ class PinnedArray:
             self.ptr = None
 
 
+# ---- asset files (hsr_obj_read / hsr_tga_read / hsr_tga_write; host only, no device) ----
+OBJ_CORNER_NORMALS = 1
+TGA_MODEL_FLIP = 1
+
+
+def obj_earlier_draws(n: int) -> int:
+    """Flag bits: with OBJ_CORNER_NORMALS, the normals of the draw after n earlier ones."""
+    return (n & 255) << 8
+
+
+def obj_read(path: str, flags: int = 0):
+    """Parse an OBJ file like Model::Model: returns (pos (n,3) f32, nrm (n,3) f32, uv (n,2) f32,
+    faces (nfaces,3,3) i32 with 0-based v/vt/vn per corner)."""
+    L = lib()
+    cnt = [ctypes.c_int32() for _ in range(4)]
+    b = str(path).encode()
+    check(L.hsr_obj_read(b, flags, None, ctypes.byref(cnt[0]), None, ctypes.byref(cnt[1]), None,
+                         ctypes.byref(cnt[2]), None, ctypes.byref(cnt[3])))
+    pos = np.empty((cnt[0].value, 3), np.float32)
+    nrm = np.empty((cnt[1].value, 3), np.float32)
+    uv = np.empty((cnt[2].value, 2), np.float32)
+    faces = np.empty((cnt[3].value, 3, 3), np.int32)
+    check(L.hsr_obj_read(b, flags, pos.ctypes.data_as(_f32p), ctypes.byref(cnt[0]), nrm.ctypes.data_as(_f32p),
+                         ctypes.byref(cnt[1]), uv.ctypes.data_as(_f32p), ctypes.byref(cnt[2]),
+                         faces.ctypes.data_as(_i32p), ctypes.byref(cnt[3])))
+    return pos, nrm, uv, faces
+
+
+def tga_read(path: str, flags: int = 0) -> np.ndarray:
+    """Read a TGA file like TGAImage::read_tga_file: returns (h, w, bytespp) u8, the buffer
+    layout (texel (x, y) at data[y, x], bytes B, G, R(, A))."""
+    L = lib()
+    w, h, bpp = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    b = str(path).encode()
+    check(L.hsr_tga_read(b, flags, None, ctypes.byref(w), ctypes.byref(h), ctypes.byref(bpp)))
+    out = np.empty((h.value, w.value, bpp.value), np.uint8)
+    check(L.hsr_tga_read(b, flags, out.ctypes.data_as(_u8p), ctypes.byref(w), ctypes.byref(h), ctypes.byref(bpp)))
+    return out
+
+
+def tga_write(path: str, data: np.ndarray, rle: bool = False) -> None:
+    """TGAImage::write_tga_file of an (h, w, bytespp) u8 buffer (top-left origin)."""
+    d = np.ascontiguousarray(data, np.uint8)
+    check(lib().hsr_tga_write(str(path).encode(), d.ctypes.data_as(_u8p), d.shape[1], d.shape[0], d.shape[2],
+                              1 if rle else 0))
+
+
 class Mesh:
-    """A Model resident on the device (hsr_mesh_upload)."""
+    """A Model resident on the device (hsr_mesh_upload, or hsr_mesh_load_obj via from_obj)."""
+
+    @classmethod
+    def from_obj(cls, path: str, flags: int = 0) -> "Mesh":
+        self = cls.__new__(cls)
+        h = ctypes.c_uint64()
+        check(lib().hsr_mesh_load_obj(str(path).encode(), flags, ctypes.byref(h)))
+        self.handle = h.value
+        self.nfaces = -1
+        return self
 
     def __init__(self, mesh):
         pos = np.ascontiguousarray(mesh.pos, np.float32)
@@ -253,7 +318,16 @@ class Mesh:
 
 
 class Texture:
-    """A TGAImage resident on the device (hsr_texture_upload)."""
+    """A TGAImage resident on the device (hsr_texture_upload, or hsr_texture_load_tga via
+    from_tga)."""
+
+    @classmethod
+    def from_tga(cls, path: str, flags: int = 0) -> "Texture":
+        self = cls.__new__(cls)
+        h = ctypes.c_uint64()
+        check(lib().hsr_texture_load_tga(str(path).encode(), flags, ctypes.byref(h)))
+        self.handle = h.value
+        return self
 
     def __init__(self, tex):
         d = np.ascontiguousarray(tex.data, np.uint8)
@@ -305,6 +379,15 @@ class Target:
                                         d.ctypes.data_as(_f32p) if d is not None else None,
                                         p.ctypes.data_as(_u32p) if p is not None else None))
         return {"color": c, "depth": d, "prim": p}
+
+    def present(self, channels: int = 3) -> np.ndarray:
+        """The image window_draw_buffer shows: top-down rows, B, G, R (, 0) per pixel."""
+        out = np.empty((self.h, self.w, channels), np.uint8)
+        check(lib().hsr_target_present(self.handle, out.ctypes.data_as(_u8p), channels))
+        return out
+
+    def write_tga(self, path: str, rle: bool = False) -> None:
+        check(lib().hsr_target_write_tga(self.handle, str(path).encode(), 1 if rle else 0))
 
     def release(self) -> None:
         if self.handle:

@@ -139,6 +139,30 @@ HSR_API int hsr_texture_upload(const uint8_t* data, int32_t w, int32_t h, int32_
                        hsr_texture* out);
 HSR_API int hsr_texture_release(hsr_texture tex);
 
+/* ---- asset files: Wavefront OBJ (Model::Model, model.cpp:6-48) and TGA
+ * (TGAImage::read_tga_file, tgaimage.cpp:40-143).  The readers run on the host and need no
+ * device (no hsr_init).  Call a reader with null arrays to get the counts, then again with
+ * arrays at least that large (the counts in/out are the capacities). */
+#define HSR_OBJ_CORNER_NORMALS 1u      /* one normal per face corner: the value Model::normal
+                                          returns there during a draw (it normalises the stored
+                                          normal in place on every read, model.cpp:108-111) ... */
+#define HSR_OBJ_EARLIER_DRAWS(n) ((uint32_t)(n) << 8)  /* ... that follows n earlier draws of the
+                                          model (0-255; a shadow pass is one: every draw reads
+                                          every corner's normal once, graphics.cpp:380-387) */
+#define HSR_TGA_MODEL_FLIP 1u          /* one more vertical flip after reading, as
+                                          Model::load_texture does for a model's maps (model.cpp:74-83) */
+/* faces: [nfaces][3 corners][v, vt, vn], 0-based, the first three corners of each face (the
+ * corners graphics_draw_triangle draws, graphics.cpp:380-387). */
+HSR_API int hsr_obj_read(const char* path, uint32_t flags, float* pos, int32_t* npos, float* nrm, int32_t* nnrm,
+                         float* uv, int32_t* nuv, int32_t* faces, int32_t* nfaces);
+/* data: w*h*bytespp bytes, the TGAImage buffer (texel (x, y) at (x + y*w)*bytespp, B,G,R(,A)). */
+HSR_API int hsr_tga_read(const char* path, uint32_t flags, uint8_t* data, int32_t* w, int32_t* h, int32_t* bytespp);
+/* TGAImage::write_tga_file (tgaimage.cpp:145-246): top-left origin, raw or run-length (rle != 0). */
+HSR_API int hsr_tga_write(const char* path, const uint8_t* data, int32_t w, int32_t h, int32_t bytespp, int32_t rle);
+/* Read and upload in one call (hsr_obj_read + hsr_mesh_upload, hsr_tga_read + hsr_texture_upload). */
+HSR_API int hsr_mesh_load_obj(const char* path, uint32_t flags, hsr_mesh* out);
+HSR_API int hsr_texture_load_tga(const char* path, uint32_t flags, hsr_texture* out);
+
 /* ---- render targets: RenderBuffer (renderbuffer.h:5-22) + a prim-id plane ------------ */
 HSR_API int hsr_target_create(int32_t w, int32_t h, hsr_target* out);
 HSR_API int hsr_target_release(hsr_target t);
@@ -147,6 +171,13 @@ HSR_API int hsr_target_clear(hsr_target t, const uint8_t rgba[4], float depth); 
 HSR_API int hsr_target_upload(hsr_target t, const uint8_t* rgba, const float* depth, const uint32_t* prim);
 /* Copy out; any pointer may be NULL.  Synchronises with the draws queued before it. */
 HSR_API int hsr_target_download(hsr_target t, uint8_t* rgba, float* depth, uint32_t* prim);
+
+/* Headless present, the pixels window_draw_buffer (win32.cpp:348-370) puts on screen: the
+ * colour plane flipped to top-down rows, bytes B, G, R per pixel (channels 3), or B, G, R, 0
+ * (channels 4; the reference never writes the fourth byte of its surface).  out holds
+ * w*h*channels bytes.  hsr_target_write_tga writes the same image as a 24-bit TGA file. */
+HSR_API int hsr_target_present(hsr_target t, uint8_t* out, int32_t channels);
+HSR_API int hsr_target_write_tga(hsr_target t, const char* path, int32_t rle);
 
 /* ---- drawing -------------------------------------------------------------------------
  * hsr_draw: one graphics_draw_triangle() call, queued on the library stream.

@@ -18,6 +18,9 @@
 //   ref_harness draw   <job.bin> <out.bin>            one frame, writes buffers
 //   ref_harness time   <job.bin> <frames>              prints ms per frame
 //   ref_harness mats   <params.bin> <out.bin>          matrix builders (maths.cpp)
+//   ref_harness obj    <file.obj> <out.bin>            Model's parse, per corner, first draw
+//   ref_harness tga    <file.tga> <model_flip> <out.bin>   TGAImage::read_tga_file (+ flip)
+//   ref_harness tgawrite <raw.bin> <rle> <out.tga>      TGAImage::write_tga_file
 #include "graphics.h"
 
 #include <chrono>
@@ -291,12 +294,62 @@ int cmd_mats(const char* inp, const char* outp) {
   return 0;
 }
 
+// Model::Model's parse as the first draw reads it: per face corner (graphics.cpp:380-387),
+// vert(i, j) (3 floats), uv(i, j) (2 floats), normal(i, j) (3 floats; the accessor
+// normalises in place, so reading in draw order gives the first draw's values).
+// out = i32 nfaces, then nfaces*3 records of 8 floats.
+int cmd_obj(const char* objp, const char* outp) {
+  Model m(objp);
+  FILE* f = std::fopen(outp, "wb");
+  if (!f) return 2;
+  int32_t nf = m.nfaces();
+  std::fwrite(&nf, 4, 1, f);
+  for (int i = 0; i < nf; i++)
+    for (int j = 0; j < 3; j++) {
+      Vector3f p = m.vert(i, j);
+      Vector2f t = m.uv(i, j);
+      Vector3f n = m.normal(i, j);
+      float rec[8] = {p.x, p.y, p.z, t.x, t.y, n.x, n.y, n.z};
+      std::fwrite(rec, 4, 8, f);
+    }
+  std::fclose(f);
+  return 0;
+}
+
+// TGAImage::read_tga_file, then (model_flip != 0) the extra flip_vertically of
+// Model::load_texture.  out = i32 w, h, bytespp, then the buffer.
+int cmd_tga(const char* tgap, int model_flip, const char* outp) {
+  TGAImage img;
+  if (!img.read_tga_file(tgap)) return 3;
+  if (model_flip) img.flip_vertically();
+  FILE* f = std::fopen(outp, "wb");
+  if (!f) return 2;
+  int32_t hdr[3] = {img.get_width(), img.get_height(), img.get_bytespp()};
+  std::fwrite(hdr, 4, 3, f);
+  std::fwrite(img.buffer(), 1, (size_t)hdr[0] * hdr[1] * hdr[2], f);
+  std::fclose(f);
+  return 0;
+}
+
+// TGAImage::write_tga_file of raw bytes: in = i32 w, h, bytespp, then the buffer.
+int cmd_tgawrite(const char* inp, int rle, const char* outp) {
+  Reader r;
+  if (!r.load(inp)) return 2;
+  int32_t w = r.get<int32_t>(), h = r.get<int32_t>(), bpp = r.get<int32_t>();
+  TGAImage img(w, h, bpp);
+  r.bytes(img.buffer(), (size_t)w * h * bpp);
+  return img.write_tga_file(outp, rle != 0) ? 0 : 3;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
+  if (argc >= 4 && std::strcmp(argv[1], "obj") == 0) return cmd_obj(argv[2], argv[3]);
+  if (argc >= 5 && std::strcmp(argv[1], "tga") == 0) return cmd_tga(argv[2], std::atoi(argv[3]), argv[4]);
+  if (argc >= 5 && std::strcmp(argv[1], "tgawrite") == 0) return cmd_tgawrite(argv[2], std::atoi(argv[3]), argv[4]);
   if (argc >= 4 && std::strcmp(argv[1], "draw") == 0) return cmd_draw(argv[2], argv[3], 0);
   if (argc >= 4 && std::strcmp(argv[1], "time") == 0) return cmd_draw(argv[2], nullptr, std::atoi(argv[3]));
   if (argc >= 4 && std::strcmp(argv[1], "mats") == 0) return cmd_mats(argv[2], argv[3]);
-  std::fprintf(stderr, "usage: ref_harness draw|time|mats ...\n");
+  std::fprintf(stderr, "usage: ref_harness draw|time|mats|obj|tga|tgawrite ...\n");
   return 2;
 }

@@ -140,3 +140,51 @@ def ref_matrices(eye, target, up, fovy, aspect, near, far, light, ortho) -> dict
         for n in os.listdir(wd):
             os.unlink(os.path.join(wd, n))
         os.rmdir(wd)
+
+
+def ref_obj_corners(obj_path: str) -> np.ndarray:
+    """Model::Model's parse read per face corner in draw order: (nfaces, 3, 8) float32 =
+    vert (3), uv (2), normal (3) as Model::normal returns it during the first draw."""
+    wd = tempfile.mkdtemp(prefix="hsrobj_")
+    try:
+        o = os.path.join(wd, "o.bin")
+        subprocess.run([HARNESS, "obj", obj_path, o], check=True, stderr=subprocess.DEVNULL)
+        data = open(o, "rb").read()
+        (nf,) = struct.unpack_from("<i", data, 0)
+        return np.frombuffer(data, np.float32, nf * 24, 4).reshape(nf, 3, 8).copy()
+    finally:
+        for n in os.listdir(wd):
+            os.unlink(os.path.join(wd, n))
+        os.rmdir(wd)
+
+
+def ref_tga_read(tga_path: str, model_flip: bool) -> np.ndarray:
+    """TGAImage::read_tga_file (+ Model::load_texture's flip): (h, w, bytespp) uint8."""
+    wd = tempfile.mkdtemp(prefix="hsrtga_")
+    try:
+        o = os.path.join(wd, "o.bin")
+        subprocess.run([HARNESS, "tga", tga_path, "1" if model_flip else "0", o], check=True, stderr=subprocess.DEVNULL)
+        data = open(o, "rb").read()
+        w, h, bpp = struct.unpack_from("<iii", data, 0)
+        return np.frombuffer(data, np.uint8, w * h * bpp, 12).reshape(h, w, bpp).copy()
+    finally:
+        for n in os.listdir(wd):
+            os.unlink(os.path.join(wd, n))
+        os.rmdir(wd)
+
+
+def ref_tga_write(img: np.ndarray, rle: bool) -> bytes:
+    """The bytes TGAImage::write_tga_file writes for an (h, w, bytespp) uint8 buffer."""
+    wd = tempfile.mkdtemp(prefix="hsrtgaw_")
+    try:
+        i = os.path.join(wd, "i.bin")
+        o = os.path.join(wd, "o.tga")
+        h, w, bpp = img.shape
+        with open(i, "wb") as f:
+            f.write(struct.pack("<iii", w, h, bpp) + np.ascontiguousarray(img, np.uint8).tobytes())
+        subprocess.run([HARNESS, "tgawrite", i, "1" if rle else "0", o], check=True, stderr=subprocess.DEVNULL)
+        return open(o, "rb").read()
+    finally:
+        for n in os.listdir(wd):
+            os.unlink(os.path.join(wd, n))
+        os.rmdir(wd)
