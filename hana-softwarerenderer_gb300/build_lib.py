@@ -20,7 +20,7 @@ LIB = os.path.join(OUT_DIR, "libhsr.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 SOURCES = ["hsr_runtime.cu", "kernels_geom.cu", "kernels_bin.cu", "kernels_raster.cu", "hsr_noalloc.cu", "hsr_serve.cu",
-           "hsr_io.cu"]
+           "hsr_io.cu", "hsr_uniforms.cpp"]
 
 NVCC_FLAGS = [ARCH, "-O3", "-lineinfo", "-std=c++17", "--fmad=false", "--prec-div=true", "--prec-sqrt=true",
               "--ftz=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2,-fvisibility=hidden",

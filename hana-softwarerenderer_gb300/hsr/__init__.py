@@ -75,6 +75,17 @@ class Request(ctypes.Structure):
                 ("out_rgba", ctypes.c_void_p), ("out_depth", ctypes.c_void_p), ("out_prim", ctypes.c_void_p)]
 
 
+class Transform(ctypes.Structure):
+    _fields_ = [("position", ctypes.c_float * 3), ("rotation", ctypes.c_float * 3), ("scale", ctypes.c_float * 3)]
+
+
+class SceneParams(ctypes.Structure):
+    _fields_ = [("camera_position", ctypes.c_float * 3), ("camera_target", ctypes.c_float * 3),
+                ("light_position", ctypes.c_float * 3), ("width", ctypes.c_int32), ("height", ctypes.c_int32),
+                ("model", Transform), ("enable_shadow", ctypes.c_int32), ("material_color", ctypes.c_float * 4),
+                ("material_specular", ctypes.c_float * 4), ("gloss", ctypes.c_float), ("bump_scale", ctypes.c_float)]
+
+
 class RequestStatus(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int32), ("batch", ctypes.c_uint32), ("batch_requests", ctypes.c_uint32),
                 ("pad", ctypes.c_uint32), ("submit_ms", ctypes.c_double), ("launch_ms", ctypes.c_double),
@@ -137,6 +148,9 @@ def lib():
                             ctypes.c_int),
         "hsr_server_now_ms": ([ctypes.c_uint64, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
         "hsr_server_destroy": ([ctypes.c_uint64], ctypes.c_int),
+        "hsr_shader_data_build": ([ctypes.POINTER(SceneParams), ctypes.c_void_p], ctypes.c_int),
+        "hsr_model_matrix": ([ctypes.POINTER(Transform), _f32p], ctypes.c_int),
+        "hsr_matrix_invert": ([_f32p, _f32p], ctypes.c_int),
         "hsr_obj_read": ([ctypes.c_char_p, ctypes.c_uint32, _f32p, _i32p, _f32p, _i32p, _f32p, _i32p, _i32p, _i32p],
                          ctypes.c_int),
         "hsr_tga_read": ([ctypes.c_char_p, ctypes.c_uint32, _u8p, _i32p, _i32p, _i32p], ctypes.c_int),
@@ -234,6 +248,47 @@ class PinnedArray:
             self.array = None
             check(lib().hsr_host_free(ctypes.c_void_p(self.ptr)))
             self.ptr = None
+
+
+# ---- uniforms (hsr_shader_data_build; host only, no device) ------------------------------
+def transform(position=(0, 0, 0), rotation=(0, 0, 0), scale=(1, 1, 1)) -> Transform:
+    t = Transform()
+    t.position[:] = [float(v) for v in position]
+    t.rotation[:] = [float(v) for v in rotation]
+    t.scale[:] = [float(v) for v in scale]
+    return t
+
+
+def shader_data_build(camera_position, width: int, height: int, *, camera_target=(0, 0, 0), light=(2, 2, 2),
+                      model: Transform | None = None, enable_shadow: bool = False, material_color=(1, 1, 1, 255),
+                      material_specular=(1, 1, 1, 255), gloss: float = 50.0, bump_scale: float = 1.0) -> np.ndarray:
+    """ShaderData as DrawModel::draw fills it (scene.h:55-71), built natively (hsr_uniforms.cpp)."""
+    p = SceneParams()
+    p.camera_position[:] = [float(v) for v in camera_position]
+    p.camera_target[:] = [float(v) for v in camera_target]
+    p.light_position[:] = [float(v) for v in light]
+    p.width, p.height = width, height
+    p.model = model if model is not None else transform()
+    p.enable_shadow = 1 if enable_shadow else 0
+    p.material_color[:] = [float(v) for v in material_color]
+    p.material_specular[:] = [float(v) for v in material_specular]
+    p.gloss, p.bump_scale = gloss, bump_scale
+    sd = np.zeros((), SHADER_DATA_DTYPE)
+    check(lib().hsr_shader_data_build(ctypes.byref(p), sd.ctypes.data))
+    return sd
+
+
+def model_matrix(t: Transform) -> np.ndarray:
+    out = np.empty(16, np.float32)
+    check(lib().hsr_model_matrix(ctypes.byref(t), out.ctypes.data_as(_f32p)))
+    return out
+
+
+def matrix_invert(m) -> np.ndarray:
+    a = np.ascontiguousarray(np.asarray(m, np.float32).reshape(16))
+    out = np.empty(16, np.float32)
+    check(lib().hsr_matrix_invert(a.ctypes.data_as(_f32p), out.ctypes.data_as(_f32p)))
+    return out
 
 
 # ---- asset files (hsr_obj_read / hsr_tga_read / hsr_tga_write; host only, no device) ----

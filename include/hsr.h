@@ -139,6 +139,29 @@ HSR_API int hsr_texture_upload(const uint8_t* data, int32_t w, int32_t h, int32_
                        hsr_texture* out);
 HSR_API int hsr_texture_release(hsr_texture tex);
 
+/* ---- uniforms: ShaderData the way DrawModel::draw fills it (scene.h:55-71), bit for bit;
+ * host only, no device needed. */
+typedef struct hsr_transform {  /* GameObject::transform (gameobject.cpp:12-17) */
+  float position[3];
+  float rotation[3];            /* degrees about x, y, z; applied as rotate_z * rotate_x * rotate_y */
+  float scale[3];
+} hsr_transform;
+typedef struct hsr_scene_params {
+  float camera_position[3];     /* Camera::position                                          */
+  float camera_target[3];       /* Camera::target (the view's look-at point)                */
+  float light_position[3];      /* light->transform.position; the light looks at the origin */
+  int32_t width, height;        /* frame buffer size: aspect = width / height                */
+  hsr_transform model;          /* the drawn GameObject                                     */
+  int32_t enable_shadow;
+  float material_color[4];      /* Material (scene.cpp:81-84): White, White, 50, 1 there     */
+  float material_specular[4];
+  float gloss;
+  float bump_scale;
+} hsr_scene_params;
+HSR_API int hsr_shader_data_build(const hsr_scene_params* p, hsr_shader_data* out);
+HSR_API int hsr_model_matrix(const hsr_transform* t, float* out16);       /* GameObject::GetModelMatrix */
+HSR_API int hsr_matrix_invert(const float* m16, float* out16);            /* Matrix4x4::invert          */
+
 /* ---- asset files: Wavefront OBJ (Model::Model, model.cpp:6-48) and TGA
  * (TGAImage::read_tga_file, tgaimage.cpp:40-143).  The readers run on the host and need no
  * device (no hsr_init).  Call a reader with null arrays to get the counts, then again with

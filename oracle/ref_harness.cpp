@@ -21,6 +21,8 @@
 //   ref_harness obj    <file.obj> <out.bin>            Model's parse, per corner, first draw
 //   ref_harness tga    <file.tga> <model_flip> <out.bin>   TGAImage::read_tga_file (+ flip)
 //   ref_harness tgawrite <raw.bin> <rle> <out.tga>      TGAImage::write_tga_file
+//   ref_harness uniforms <params.bin> <out.bin>         model matrix + DrawModel::draw uniforms
+#include "camera.h"
 #include "graphics.h"
 
 #include <chrono>
@@ -341,15 +343,60 @@ int cmd_tgawrite(const char* inp, int rle, const char* outp) {
   return img.write_tga_file(outp, rle != 0) ? 0 : 3;
 }
 
+// GameObject::GetModelMatrix (gameobject.cpp:12-17) for a transform, its inverse
+// (Matrix4x4::invert) and DrawModel::draw's uniforms (scene.h:55-71) for a camera and light:
+// in = f32 position[3], rotation_deg[3], scale[3], eye[3], target[3], light[3], i32 w, h
+// out = model, model_I, view, proj, light_vp, camera_vp (16 floats each), light_dir (3)
+int cmd_uniforms(const char* inp, const char* outp) {
+  Reader r;
+  if (!r.load(inp)) return 2;
+  Vector3f pos, rot, scl, eye, target, light;
+  read_vec3(r, pos); read_vec3(r, rot); read_vec3(r, scl);
+  read_vec3(r, eye); read_vec3(r, target); read_vec3(r, light);
+  int32_t w = r.get<int32_t>(), h = r.get<int32_t>();
+  // the composition of GameObject::GetModelMatrix
+  Matrix4x4 m_translation = translate(pos.x, pos.y, pos.z);
+  Matrix4x4 m_rotate = rotate_z(TO_RADIANS(rot.z)) * rotate_x(TO_RADIANS(rot.x)) * rotate_y(TO_RADIANS(rot.y));
+  Matrix4x4 m_scale = scale(scl.x, scl.y, scl.z);
+  Matrix4x4 model = m_translation * m_rotate * m_scale;
+  Matrix4x4 model_I = model.invert();
+  // Camera::get_view_matrix / get_proj_matrix (camera.cpp:82-92), DrawModel::draw (scene.h:55-71)
+  Camera cam(eye, target, (float)w / (float)h);
+  Matrix4x4 view = cam.get_view_matrix();
+  Matrix4x4 proj = cam.get_proj_matrix();
+  float aspect = (float)w / (float)h;
+  Matrix4x4 lvp = orthographic(aspect, 1, 0, 5) * lookat(light, cam.get_target_position(), Vector3f(0, 1, 0));
+  Matrix4x4 cvp = proj * view;
+  Vector3f ld = (light - cam.get_target_position()).normalize();
+  FILE* f = std::fopen(outp, "wb");
+  if (!f) return 2;
+  Matrix4x4* ms[6] = {&model, &model_I, &view, &proj, &lvp, &cvp};
+  for (Matrix4x4* m : ms)
+    for (int i = 0; i < 4; i++)
+      for (int j = 0; j < 4; j++) { float v = (*m)[i][j]; std::fwrite(&v, 4, 1, f); }
+  float l3[3] = {ld.x, ld.y, ld.z};
+  std::fwrite(l3, 4, 3, f);
+  std::fclose(f);
+  return 0;
+}
+
 }  // namespace
 
+// camera.cpp's interactive update_camera reads the Win32 input layer (win32.cpp), which is
+// not built headless; the harness never calls it, so these stand-ins only satisfy the linker.
+void input_query_cursor(window_t*, float* xpos, float* ypos) { *xpos = 0.f; *ypos = 0.f; }
+int input_key_pressed(window_t*, keycode_t) { return 0; }
+void* window_get_userdata(window_t*) { return nullptr; }
+float platform_get_time(void) { return 0.f; }
+
 int main(int argc, char** argv) {
+  if (argc >= 4 && std::strcmp(argv[1], "uniforms") == 0) return cmd_uniforms(argv[2], argv[3]);
   if (argc >= 4 && std::strcmp(argv[1], "obj") == 0) return cmd_obj(argv[2], argv[3]);
   if (argc >= 5 && std::strcmp(argv[1], "tga") == 0) return cmd_tga(argv[2], std::atoi(argv[3]), argv[4]);
   if (argc >= 5 && std::strcmp(argv[1], "tgawrite") == 0) return cmd_tgawrite(argv[2], std::atoi(argv[3]), argv[4]);
   if (argc >= 4 && std::strcmp(argv[1], "draw") == 0) return cmd_draw(argv[2], argv[3], 0);
   if (argc >= 4 && std::strcmp(argv[1], "time") == 0) return cmd_draw(argv[2], nullptr, std::atoi(argv[3]));
   if (argc >= 4 && std::strcmp(argv[1], "mats") == 0) return cmd_mats(argv[2], argv[3]);
-  std::fprintf(stderr, "usage: ref_harness draw|time|mats|obj|tga|tgawrite ...\n");
+  std::fprintf(stderr, "usage: ref_harness draw|time|mats|obj|tga|tgawrite|uniforms ...\n");
   return 2;
 }

@@ -188,3 +188,25 @@ def ref_tga_write(img: np.ndarray, rle: bool) -> bytes:
         for n in os.listdir(wd):
             os.unlink(os.path.join(wd, n))
         os.rmdir(wd)
+
+
+def ref_uniforms(position, rotation_deg, scale, eye, target, light, width: int, height: int) -> dict:
+    """GameObject::GetModelMatrix, its inverse, and DrawModel::draw's matrices and light
+    direction from the reference (camera.cpp, maths.cpp, scene.h:55-71)."""
+    wd = tempfile.mkdtemp(prefix="hsruni_")
+    try:
+        p = os.path.join(wd, "p.bin")
+        o = os.path.join(wd, "o.bin")
+        vals = list(position) + list(rotation_deg) + list(scale) + list(eye) + list(target) + list(light)
+        with open(p, "wb") as f:
+            f.write(np.array(vals, np.float32).tobytes() + struct.pack("<ii", width, height))
+        subprocess.run([HARNESS, "uniforms", p, o], check=True)
+        a = np.fromfile(o, np.float32)
+        names = ["model", "model_I", "view", "proj", "light_vp", "camera_vp"]
+        out = {n: a[16 * k:16 * (k + 1)] for k, n in enumerate(names)}
+        out["light_dir"] = a[96:99]
+        return out
+    finally:
+        for n in os.listdir(wd):
+            os.unlink(os.path.join(wd, n))
+        os.rmdir(wd)

@@ -68,6 +68,8 @@ def test_struct_layouts_match_header(tmp_path):
         "hsr_timing": (hsr.Timing, ["launches", "h2d_bytes", "clipped_faces", "fragments"]),
         "hsr_stats": (hsr.Stats, ["kernel_launches"]),
         "hsr_tuning": (hsr.Tuning, ["bin_factor"]),
+        "hsr_transform": (hsr.Transform, ["rotation", "scale"]),
+        "hsr_scene_params": (hsr.SceneParams, ["width", "model", "enable_shadow", "gloss", "bump_scale"]),
     }
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "hsr.h"', "int main(void) {"]
     for cname, (_, fields) in checks.items():

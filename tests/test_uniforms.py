@@ -1,0 +1,70 @@
+"""CPU: the native uniform builder (hsr_shader_data_build, hsr_model_matrix, hsr_matrix_invert)
+gives the reference's bits — against the golden matrices (generated from the reference's
+maths.cpp), against the Python builder, and, where the reference sources are present, against
+the reference's own GameObject::GetModelMatrix / Camera / DrawModel::draw built headless.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import golden_io
+import hsr
+import refjob
+from hsr import uniforms as U
+
+needs_ref = pytest.mark.skipif(not refjob.available(), reason="reference sources not present on this host")
+
+FIELDS = ("view_pos", "light_dir", "light_color", "ambient", "model_matrix", "model_matrix_I", "view_matrix",
+          "projection_matrix", "light_vp_matrix", "camera_vp_matrix", "enable_shadow", "material_color",
+          "material_specular", "gloss", "bump_scale")
+
+
+def bits(x):
+    return np.asarray(x, np.float32).reshape(-1).view(np.uint32)
+
+
+def test_matches_golden_matrices():
+    rows = np.load(os.path.join(golden_io.GOLDEN, "matrices.npy"))
+    for r in rows:
+        eye, (w, h) = tuple(float(x) for x in r[0:3]), (int(r[3]), int(r[4]))
+        sd = hsr.shader_data_build(eye, w, h)
+        exp = {"view_matrix": r[5:21], "projection_matrix": r[21:37], "camera_vp_matrix": r[37:53],
+               "light_vp_matrix": r[53:69], "model_matrix_I": r[69:85], "light_dir": r[85:88]}
+        for k, v in exp.items():
+            assert np.array_equal(bits(sd[k]), bits(v)), (eye, k)
+
+
+@pytest.mark.parametrize("eye,w,h", [((0, 0, 3), 512, 512), ((0.3, 0.8, 3.2), 1920, 1080), ((-2.5, 1.5, 1.0), 137, 2160)])
+def test_matches_python_builder(eye, w, h):
+    a = hsr.shader_data_build(eye, w, h, enable_shadow=True)
+    b = U.shader_data(eye, w, h, enable_shadow=True)
+    for k in FIELDS:
+        assert np.array_equal(np.asarray(a[k]).reshape(-1).view(np.uint32), np.asarray(b[k]).reshape(-1).view(np.uint32)), k
+
+
+def test_invert_of_identity_has_the_reference_signed_zeros():
+    inv = hsr.matrix_invert(np.eye(4, dtype=np.float32))
+    py = U.Mat4.identity().invert().flat()
+    assert np.array_equal(bits(inv), bits(py))
+
+
+@needs_ref
+def test_matches_reference_model_camera_and_light():
+    rng = np.random.default_rng(12)
+    for _ in range(60):
+        pos = rng.uniform(-3, 3, 3).astype(np.float32)
+        rot = rng.uniform(-400, 400, 3).astype(np.float32)
+        scl = rng.uniform(0.2, 3, 3).astype(np.float32) * rng.choice([-1, 1], 3)
+        eye = rng.uniform(-4, 4, 3).astype(np.float32)
+        target = rng.uniform(-0.5, 0.5, 3).astype(np.float32)
+        light = rng.uniform(-4, 4, 3).astype(np.float32) + np.float32(0.1)
+        w, h = int(rng.integers(64, 4000)), int(rng.integers(64, 2200))
+        ref = refjob.ref_uniforms(pos, rot, scl, eye, target, light, w, h)
+        t = hsr.transform(pos, rot, scl)
+        assert np.array_equal(bits(hsr.model_matrix(t)), bits(ref["model"]))
+        sd = hsr.shader_data_build(eye, w, h, camera_target=target, light=light, model=t)
+        for k, rk in (("model_matrix", "model"), ("model_matrix_I", "model_I"), ("view_matrix", "view"),
+                      ("projection_matrix", "proj"), ("light_vp_matrix", "light_vp"),
+                      ("camera_vp_matrix", "camera_vp"), ("light_dir", "light_dir")):
+            assert np.array_equal(bits(sd[k]), bits(ref[rk])), k
