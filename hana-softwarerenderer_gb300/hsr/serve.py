@@ -89,35 +89,53 @@ class ViewBatch:
 
 
 class PinnedRing:
-    """Page-locked output buffers carved from one ring; a region is reused only after the
-    request that owns it has completed."""
+    """Page-locked output buffers carved from one ring in allocation order; a region is
+    reused only after the request that owns it has completed.  Allocation and release are
+    O(1): regions are handed out and reclaimed first in, first out."""
 
     def __init__(self, nbytes: int):
         self.buf = PinnedArray((nbytes,), np.uint8)
         self.cap = nbytes
-        self.head = 0
-        self.live: collections.deque = collections.deque()  # (ticket-ish key, start, end)
+        self.head = 0                                     # next free byte
+        self.live: collections.deque = collections.deque()  # [key, start, end, freed] in allocation order
+        self.by_key: dict = {}
+
+    def _drop_freed(self) -> None:
+        while self.live and self.live[0][3]:
+            del self.by_key[self.live.popleft()[0]]
+
+    def _fits(self, n: int) -> int:
+        """Start of a free region of n bytes at the head (or the ring's start), or -1."""
+        if not self.live:
+            return self.head if self.head + n <= self.cap else 0
+        s0 = self.live[0][1]
+        if self.head > s0:
+            if self.head + n <= self.cap:
+                return self.head
+            return 0 if n <= s0 else -1
+        return self.head if self.head + n <= s0 else -1
 
     def alloc(self, n: int, key, reclaim) -> np.ndarray:
         n = (n + 255) // 256 * 256
         if n > self.cap:
             raise ValueError("request output larger than the pinned ring")
         while True:
-            start = self.head if self.head + n <= self.cap else 0
-            end = start + n
-            busy = any(not (e <= start or s >= end) for _, s, e in self.live)
-            if not busy:
+            self._drop_freed()
+            start = self._fits(n)
+            if start >= 0:
                 break
             reclaim()  # waits for the oldest outstanding request
-        self.head = end
-        self.live.append((key, start, end))
-        return self.buf.array[start:end]
+        self.head = start + n
+        entry = [key, start, start + n, False]
+        self.live.append(entry)
+        self.by_key[key] = entry
+        return self.buf.array[start:start + n]
 
     def free(self, key) -> None:
-        for i, (k, _, _) in enumerate(self.live):
-            if k == key:
-                del self.live[i]
-                return
+        e = self.by_key.get(key)
+        if e is not None:
+            e[3] = True
+        self._drop_freed()
 
     def release(self) -> None:
         self.buf.release()
