@@ -110,7 +110,7 @@ struct __align__(128) DView {
   int32_t vch_base, vch_npos, vch_count;
   int32_t sch_base;
 };
-constexpr int kVertexChunk = 1024;  // positions or normals per vertex-stage chunk
+constexpr int kVertexChunk = 2048;  // positions or normals per vertex-stage chunk
 constexpr int kSetupChunk = 256;    // faces per setup chunk (one per thread of a block)
 static_assert(offsetof(DView, prim_base) + sizeof(uint32_t) <= 128, "per-tile fields must share one line");
 

@@ -149,42 +149,57 @@ __device__ __forceinline__ Chunk setup_chunk(const DView* views, const int32_t* 
 // ---------------------------------------------------------------------------------------
 // vertex stage
 // ---------------------------------------------------------------------------------------
-// One vertex chunk (kVertexChunk items, 4 per thread).
+// One vertex chunk (kVertexChunk items, 8 per thread, 256 threads).
 __device__ __forceinline__ void vertex_chunk_work(const DView& v, const Chunk& ch) {
-  const int i4 = ch.begin + (int)threadIdx.x * 4;
-  if (i4 >= ch.end) return;
+  // item i = begin + threadIdx.x + 256 k: consecutive threads read consecutive floats and
+  // write consecutive float4s, so every load and store instruction of a warp is one
+  // contiguous span; the four loads of a thread are issued before any is used
+  constexpr int kPer = kVertexChunk / 256;
+  const int i0 = ch.begin + (int)threadIdx.x;
   if (ch.kind == 0) {
     // positions: ObjectToClipPos / ObjectToViewPos (IShader.h:55-61), ObjectToWorldPos (:63-65)
-    const float4 X = __ldg(reinterpret_cast<const float4*>(v.px + i4));
-    const float4 Y = __ldg(reinterpret_cast<const float4*>(v.py + i4));
-    const float4 Z = __ldg(reinterpret_cast<const float4*>(v.pz + i4));
-    const float xs[4] = {X.x, X.y, X.z, X.w}, ys[4] = {Y.x, Y.y, Y.z, Y.w}, zs[4] = {Z.x, Z.y, Z.z, Z.w};
+    float xs[kPer], ys[kPer], zs[kPer];
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-      if (i4 + k >= ch.end) break;
-      v.sv[i4 + k] = screen_vertex(mat_vec(v.mvp, xs[k], ys[k], zs[k], 1.f));
+    for (int k = 0; k < kPer; k++) {
+      const int i = i0 + 256 * k;
+      const bool in = i < ch.end;
+      xs[k] = in ? __ldg(v.px + i) : 0.f;
+      ys[k] = in ? __ldg(v.py + i) : 0.f;
+      zs[k] = in ? __ldg(v.pz + i) : 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+      const int i = i0 + 256 * k;
+      if (i >= ch.end) break;
+      v.sv[i] = screen_vertex(mat_vec(v.mvp, xs[k], ys[k], zs[k], 1.f));
       if (v.wpos) {
-        float4 w = mat_vec(v.u.model_matrix, xs[k], ys[k], zs[k], 1.f);
-        v.wpos[i4 + k] = make_float4(w.x, w.y, w.z, 0.f);
+        const float4 w = mat_vec(v.u.model_matrix, xs[k], ys[k], zs[k], 1.f);
+        v.wpos[i] = make_float4(w.x, w.y, w.z, 0.f);
       }
     }
   } else {
     // normals: ObjectToWorldNormal (IShader.h:71-75) = [n, 1] * model_I; intensity of
     // Ground/Toon = saturate(worldN . light_dir) (IShader.cpp:8, :26)
-    const float4 X = __ldg(reinterpret_cast<const float4*>(v.nx + i4));
-    const float4 Y = __ldg(reinterpret_cast<const float4*>(v.ny + i4));
-    const float4 Z = __ldg(reinterpret_cast<const float4*>(v.nz + i4));
-    const float xs[4] = {X.x, X.y, X.z, X.w}, ys[4] = {Y.x, Y.y, Y.z, Y.w}, zs[4] = {Z.x, Z.y, Z.z, Z.w};
+    float xs[kPer], ys[kPer], zs[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+      const int i = i0 + 256 * k;
+      const bool in = i < ch.end;
+      xs[k] = in ? __ldg(v.nx + i) : 0.f;
+      ys[k] = in ? __ldg(v.ny + i) : 0.f;
+      zs[k] = in ? __ldg(v.nz + i) : 0.f;
+    }
     const float* m = v.u.model_matrix_I;
     const F3 L = {v.u.light_dir[0], v.u.light_dir[1], v.u.light_dir[2]};
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-      if (i4 + k >= ch.end) break;
+    for (int k = 0; k < kPer; k++) {
+      const int i = i0 + 256 * k;
+      if (i >= ch.end) break;
       F3 wn;
       wn.x = dot4(xs[k], ys[k], zs[k], 1.f, m[0], m[4], m[8], m[12]);
       wn.y = dot4(xs[k], ys[k], zs[k], 1.f, m[1], m[5], m[9], m[13]);
       wn.z = dot4(xs[k], ys[k], zs[k], 1.f, m[2], m[6], m[10], m[14]);
-      v.wnrm[i4 + k] = make_float4(wn.x, wn.y, wn.z, saturate(dot3(wn, L)));
+      v.wnrm[i] = make_float4(wn.x, wn.y, wn.z, saturate(dot3(wn, L)));
     }
   }
 }
