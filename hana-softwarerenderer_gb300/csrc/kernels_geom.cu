@@ -559,7 +559,7 @@ __device__ __forceinline__ void face_payload(const DView& v, int f, int nf4, Pay
 // shading payload, the tile counts, and the hand-over of huge triangles to k_big (their
 // slot becomes a hole the binning skips).  Grid-stride with warp-uniform trip counts, so
 // the warp collectives of append_small see every lane.
-__global__ void __launch_bounds__(kSetupThreads) k_emit(const DView* __restrict__ views, int T, Scratch sc) {
+__global__ void __launch_bounds__(kSetupThreads, 4) k_emit(const DView* __restrict__ views, int T, Scratch sc) {
   const int lane = threadIdx.x & 31;
   if (sc.ctl->error & kErrCapacity) return;
   const uint32_t nrec = min(sc.ctl->rec_count, sc.rec_cap);
