@@ -367,7 +367,8 @@ def run_frame(args) -> dict:
     g = hframe.GpuFrame(fr)
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
     old = hsr.get_tuning()
-    hsr.autotune(g.descs, reps=3)
+    if not args.tile:
+        hsr.autotune(g.descs, reps=3)
     hsr.set_profiling(True)
     for _ in range(3):
         g.render()
@@ -414,7 +415,7 @@ def run_soup(args) -> dict:
     g = hframe.GpuFrame(fr)
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
     old = hsr.get_tuning()
-    tuned = hsr.autotune(g.descs, reps=2)
+    tuned = hsr.autotune(g.descs, reps=2) if not args.tile else None
     hsr.set_profiling(True)
     for _ in range(3):
         g.render()
@@ -574,11 +575,24 @@ def main():
     ap.add_argument("--warps", type=int, default=0, help="with --tile: warps per CTA of the raster (4 or 8)")
     ap.add_argument("--ctas", type=int, default=0, help="with --tile: raster CTAs per SM")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--only", choices=["frame", "views", "soup"], default=None,
+                    help="run one sub-workload alone and print its result (for profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
     if args.impl == "reference":
         out = run_reference(args, world, rank)
+    elif args.only:
+        import torch
+
+        import hsr
+
+        torch.cuda.set_device(local)
+        hsr.init(local)
+        if args.tile:
+            hsr.set_tuning(tile=args.tile, warps_per_cta=args.warps or (4 if args.tile == 16 else 8),
+                           ctas_per_sm=args.ctas or None)
+        out = {"frame": run_frame, "views": run_views, "soup": run_soup}[args.only](args)
     else:
         out = run_ours(args, world, rank, local)
     if rank == 0 and out is not None:
