@@ -142,6 +142,27 @@ __device__ __forceinline__ bool cover_test(float ax, float ay, float e1x, float 
   return !(b0 < 0.f || b1 < 0.f || b2 < 0.f);
 }
 
+// (float)sqrt(1.0 - (double)s) for s = saturate(...) — the bump height of NormalMapShader
+// (IShader.cpp:143), which the reference evaluates in double — in single precision (FP64 runs at
+// a small fraction of the FP32 rate on this part).  For s >= 2^-29, 1 - s is exactly hi + lo
+// (Fast2Sum); y = sqrtf(hi) is refined by one Newton step on the exact FMA residual hi - y*y
+// (the correction step of Markstein's square root), which gives the correctly rounded square
+// root of hi + lo except where it lands on a rounding midpoint.  Checked against the double
+// expression for every float s in [0, 1] (tests/cuda/bump_z_check.cu): it differs only at
+// s = 1 (0/0 in the correction: the answer is 0) and s = 2^-24 (1 - 2^-24 exactly; its square
+// root lies 2^-51 below the midpoint 1 - 2^-25 that the float correction reaches); below 2^-29
+// every s gives 1.  NaN keeps the double expression.
+__device__ __forceinline__ float bump_height(float s) {
+  if (!(s >= 0x1p-29f)) return s != s ? __double2float_rn(__dsqrt_rn(__dsub_rn(1.0, (double)s))) : 1.f;
+  if (s == 1.f) return 0.f;
+  if (s == 0x1p-24f) return 0x1.fffffep-1f;
+  const float hi = __fsub_rn(1.f, s);
+  const float lo = __fsub_rn(__fsub_rn(1.f, hi), s);  // exact: 1 - s = hi + lo
+  const float y = __fsqrt_rn(hi);
+  const float e = __fmaf_rn(-y, y, hi);              // exact residual hi - y*y
+  return __fadd_rn(y, __fdiv_rn(__fadd_rn(e, lo), __fadd_rn(y, y)));
+}
+
 // viewport_transform (maths.cpp:20-25)
 __device__ __forceinline__ F3 viewport(int32_t w, int32_t h, F3 ndc) {
   return {fm(fm(fa(ndc.x, 1.f), 0.5f), (float)w), fm(fm(fa(ndc.y, 1.f), 0.5f), (float)h), fm(fa(ndc.z, 1.f), 0.5f)};
@@ -253,7 +274,7 @@ __device__ __forceinline__ Col fragment_s(const DView& v, const float* P, float 
             bump.x = fm(bump.x, v.u.bump_scale);
             bump.y = fm(bump.y, v.u.bump_scale);
             float bb = fa(fa(0.f, fm(bump.y, bump.y)), fm(bump.x, bump.x));
-            bump.z = __double2float_rn(__dsqrt_rn(__dsub_rn(1.0, (double)saturate(bb))));
+            bump.z = bump_height(saturate(bb));  // (float)sqrt(1.0 - saturate(bb)) in double, IShader.cpp:143
             F3 tn = {dot3(r0, bump), dot3(r1, bump), dot3(r2, bump)};
             return lit(v, normalize3(tn), wp, u, t, bt);
           }
