@@ -238,13 +238,16 @@ __device__ __forceinline__ Col fragment_s(const DView& v, const float* P, float 
       return c_mulf(white, interp(P[3], P[4], P[5], w0, w1, w2, nrm));
     } else if constexpr (S == HSR_SHADER_GROUND) {  // IShader.cpp:12-15
       return c_mulf(white, interp(P[3], P[4], P[5], w0, w1, w2, nrm));
-    } else if constexpr (S == HSR_SHADER_TOON) {  // IShader.cpp:30-39 (double compares, as written)
+    } else if constexpr (S == HSR_SHADER_TOON) {  // IShader.cpp:30-39
+      // The reference compares the float against double constants: (double)f > c holds exactly
+      // when f > the largest float not above c (none of these constants is a float), so each
+      // compare runs in single precision with that float.
       float intensity = interp(P[3], P[4], P[5], w0, w1, w2, nrm);
-      if ((double)intensity > .85) intensity = 1.f;
-      else if ((double)intensity > .60) intensity = (float).80;
-      else if ((double)intensity > .45) intensity = (float).60;
-      else if ((double)intensity > .30) intensity = (float).45;
-      else if ((double)intensity > .15) intensity = (float).30;
+      if (intensity > 0x1.b33332p-1f) intensity = 1.f;               // .85
+      else if (intensity > 0x1.333332p-1f) intensity = (float).80;   // .60
+      else if (intensity > 0x1.ccccccp-2f) intensity = (float).60;   // .45
+      else if (intensity > 0x1.333332p-2f) intensity = (float).45;   // .30
+      else if (intensity > 0x1.333332p-3f) intensity = (float).30;   // .15
       Col base = {1.f, fd(155.f, 255.f), 0.f, 255.f};
       return c_mulf(base, intensity);
     } else {

@@ -43,3 +43,18 @@ def test_prim_ids_are_faces_plus_one():
     frame, exp = golden_io.load("soup_ties_12k")
     prim = exp["main"]["prim"]
     assert prim.max() <= frame.mesh.nfaces and (prim > 0).sum() > 0
+
+
+def test_toon_single_precision_thresholds():
+    """The device Toon shader compares the float intensity against the largest float not above
+    each double constant of IShader.cpp:30-39; (double)f > c holds exactly when f > that float."""
+    import re
+
+    src = open(os.path.join(os.path.dirname(golden_io.GOLDEN), "..", "hana-softwarerenderer_gb300", "csrc",
+                            "hsr_device.cuh")).read()
+    found = re.findall(r"intensity > (0x[0-9a-f.]+p-\d)f\) intensity = [^;]+;\s+// (\.\d\d)", src)
+    assert [c for _, c in found] == [".85", ".60", ".45", ".30", ".15"]
+    for h, c in found:
+        f = np.float32(float.fromhex(h))
+        assert float(f) == float.fromhex(h)
+        assert float(f) <= float(c) < float(np.nextafter(f, np.float32(1)))
