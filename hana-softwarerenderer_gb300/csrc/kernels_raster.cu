@@ -84,23 +84,30 @@ struct BatchRecs {
   float ax[32], ay[32], e1x[32], e1y[32], e2x[32], e2y[32], uz[32], d0[32], d1[32], d2[32];
   uint32_t seq[32];    // submission order
   uint32_t idx[32];    // record index
+  uint32_t pay[32];    // payload index (read by tiles that keep the winner's weights)
   uint32_t off[32];    // first candidate of the record's run
   uint32_t box[32];    // box in the tile: x0 | y0 << 8 | width << 16, bit 31 = kRecExact
   uint32_t magic[32];  // ceil(65536 / width): row of a candidate by multiply-shift
 };
 
 // Per-warp tile state in shared memory: per pixel the key (ordered depth | submission) and
-// the index of the record that holds it.
+// the index of the record that holds it.  8x8 tiles also keep the winner's payload index,
+// submission number and barycentric weights (28 bytes a pixel), so shading reads no record;
+// 16x16 tiles keep 12 bytes a pixel, which leaves room for 8 warps of them per SM, and
+// shading evaluates the weights again from the record.
 template <int NPIX>
 struct TileState {
+  static constexpr bool kKeep = NPIX <= 64;
   unsigned long long key[NPIX];
   uint32_t rec[NPIX];
+  uint32_t pay[kKeep ? NPIX : 1], seq[kKeep ? NPIX : 1];
+  float b0[kKeep ? NPIX : 1], b1[kKeep ? NPIX : 1], b2[kKeep ? NPIX : 1];
 };
 
 // Shade the winners of one tile and write colour, depth and prim id (fused clear writes the
-// clear values where nothing won).  S is the shader, known at compile time.  The winner's
-// barycentric weights are evaluated again from its record: the same operations on the same
-// values as in the visibility pass, so the same bits.
+// clear values where nothing won).  S is the shader, known at compile time.  Without kept
+// weights (16x16 tiles) the winner's barycentric weights are evaluated again from its record:
+// the same operations on the same values as in the visibility pass, so the same bits.
 template <int T, int S>
 __device__ __forceinline__ uint32_t shade_tile(const DView& v, const Scratch& sc, const TileState<T * T>& st, int ox,
                                                int oy, bool clear, const ByteTables& bt) {
@@ -117,17 +124,26 @@ __device__ __forceinline__ uint32_t shade_tile(const DView& v, const Scratch& sc
     const uint32_t ri = st.rec[p];
     if (ri != kNone) {
       shaded++;
-      const RasterRec r = sc.recs[ri];
       float b0, b1, b2;
-      cover_test(r.ax, r.ay, r.e1x, r.e1y, r.e2x, r.e2y, r.uz, ((r.view >> kRecFlagShift) & kRecExact) != 0u, (float)x,
-                 (float)y, b0, b1, b2);
+      uint32_t pay, seq;
+      if constexpr (TileState<T * T>::kKeep) {
+        b0 = st.b0[p]; b1 = st.b1[p]; b2 = st.b2[p];
+        pay = st.pay[p];
+        seq = st.seq[p];
+      } else {
+        const RasterRec r = sc.recs[ri];
+        cover_test(r.ax, r.ay, r.e1x, r.e1y, r.e2x, r.e2y, r.uz, ((r.view >> kRecFlagShift) & kRecExact) != 0u,
+                   (float)x, (float)y, b0, b1, b2);
+        pay = r.pad;
+        seq = r.seq;
+      }
       float P[NF4 > 0 ? NF4 * 4 : 4];
       if constexpr (NF4 > 0) {
-        const float4* src = reinterpret_cast<const float4*>(&sc.pay[r.pad]);
+        const float4* src = reinterpret_cast<const float4*>(&sc.pay[pay]);
 #pragma unroll
         for (int k = 0; k < NF4; k++) reinterpret_cast<float4*>(P)[k] = src[k];
       }
-      const uint32_t prim = v.prim_base + (r.seq >> 4) + 1u;
+      const uint32_t prim = v.prim_base + (seq >> 4) + 1u;
       const uint32_t alpha = clear ? v.clear_rgba : __ldcg(&v.color[idx]);
       v.color[idx] = pack_rgb(fragment_s<S>(v, P, b0, b1, b2, prim, bt), alpha);
       v.depth[idx] = from_ord((uint32_t)(st.key[p] >> 32));
@@ -272,6 +288,7 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
           br.d0[k] = rr.d0; br.d1[k] = rr.d1; br.d2[k] = rr.d2;
           br.seq[k] = rr.seq;
           br.idx[k] = ri;
+          if constexpr (TileState<NPIX>::kKeep) br.pay[k] = rr.pad;
           br.off[k] = start;
           br.box[k] = box | (((rr.view >> kRecFlagShift) & kRecExact) ? 0x80000000u : 0u);
           br.magic[k] = kDivMagic[box >> 16];
@@ -286,6 +303,7 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
           bool covered = false;
           unsigned long long key = 0ull, old = 0ull;
           int p = 0, j = 0;
+          float b0 = 0.f, b1 = 0.f, b2 = 0.f;
           if (i < W) {
             // owner: the last run starting at or before candidate i
             j = (int)(before + (uint32_t)__popc(here & ((2u << lane) - 1u))) - 1;
@@ -296,7 +314,6 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
             const int lx = (int)(bx & 255u) + (int)(q - qy * lw);
             const int ly = (int)((bx >> 8) & 255u) + (int)qy;
             p = ly * T + lx;
-            float b0, b1, b2;
             covered = cover_test(br.ax[j], br.ay[j], br.e1x[j], br.e1y[j], br.e2x[j], br.e2y[j], br.uz[j],
                                  (bx >> 31) != 0u, (float)(ox + lx), (float)(oy + ly), b0, b1, b2);
             if (covered) {
@@ -308,7 +325,16 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
             }
           }
           __syncwarp();
-          if (covered && old > key && st.key[p] == key) st.rec[p] = br.idx[j];
+          if (covered && old > key && st.key[p] == key) {
+            st.rec[p] = br.idx[j];
+            if constexpr (TileState<NPIX>::kKeep) {
+              st.pay[p] = br.pay[j];
+              st.seq[p] = br.seq[j];
+              st.b0[p] = b0;
+              st.b1[p] = b1;
+              st.b2[p] = b2;
+            }
+          }
           __syncwarp();
         }
       }
