@@ -222,7 +222,7 @@ int launch_vertex(const DView* views, int nviews, int nchunks, int grid, cudaStr
 // ---------------------------------------------------------------------------------------
 // setup stage
 // ---------------------------------------------------------------------------------------
-constexpr int kSetupCoverPixels = 8;  // pixel ranges up to this size are tested in setup
+constexpr int kSetupCoverPixels = 12;  // pixel ranges up to this size are tested in setup
 
 __device__ __forceinline__ bool coord_ok(float c) {
   float a = fabsf(c);
