@@ -95,10 +95,10 @@ int Arena::reserve(size_t bytes) {
 
 int Pinned::reserve(size_t bytes) {
   if (bytes <= cap) return HSR_OK;
+  const size_t want = std::max({bytes, cap + cap / 2, (size_t)1 << 16});
   if (base) cudaFreeHost(base);
   base = nullptr;
   cap = 0;
-  size_t want = std::max(bytes, (size_t)1 << 16);
   cudaError_t e = cudaMallocHost((void**)&base, want);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -366,6 +366,13 @@ bool Plan::grow(const Ctl& c) {
   return true;
 }
 
+void Runtime::learn_caps(const Plan& p) {
+  cap_rec_hint = std::max(cap_rec_hint, p.rec_cap);
+  cap_clip_hint = std::max(cap_clip_hint, p.clip_cap);
+  cap_bin_hint = std::max(cap_bin_hint, p.bin_cap);
+  cap_big_hint = std::max(cap_big_hint, p.big_cap);
+}
+
 void Runtime::record_result(const Plan& p, const Ctl& c) {
   stats.records = c.rec_count;
   stats.clipped_faces = c.clip_count;
@@ -409,7 +416,7 @@ int Runtime::run_batch(const hsr_draw_desc* descs, int n) {
     const Ctl c = *(const Ctl*)(p.host + p.host_bytes);
     if (p.grow(c)) {
       stats.retries++;
-      cap_rec_hint = p.rec_cap; cap_clip_hint = p.clip_cap; cap_bin_hint = p.bin_cap; cap_big_hint = p.big_cap;
+      learn_caps(p);
       continue;
     }
     if (c.error & (kErrWaitTimeout | kErrScanTimeout))

@@ -101,6 +101,9 @@ struct Runtime {
                  std::vector<int>& dep1);
   int plan_build(const hsr_draw_desc* descs, int n, Plan& p);
   void record_result(const Plan& p, const Ctl& c);
+  // A plan overflowed and grew: later plans start from at least its capacities (every path
+  // that launches plans, so one overflow is not repeated by each later batch).
+  void learn_caps(const Plan& p);
   int run_batch(const hsr_draw_desc* descs, int n);
   int clear_target(TargetObj* t, const uint8_t rgba[4], float depth);
 

@@ -8,8 +8,11 @@
 //     staging the graph's upload node reads at launch time;
 //   - a server turns independently arriving requests into batches: a scheduler thread
 //     admits queued requests while the framebuffer pool has room, packs everything admitted
-//     into one launch sequence on a free slot (stream), and completes requests as their
-//     batch's event fires.  Several slots keep batches overlapping on the device.
+//     into one launch sequence on a free slot, and completes requests as their batch's event
+//     fires.  A slot is one batch in flight: launch sequences run one after another on the
+//     server's compute stream (two launch sequences sharing the SMs finish later than the same
+//     two in turn), while the host forms the next batch and each slot's copy stream brings its
+//     results back under the next batch's kernels.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -108,6 +111,7 @@ static int plan_wait(Runtime* rt, PlanObj* po) {
     const Ctl c = *(const Ctl*)(po->p.host + po->p.host_bytes);
     if (po->p.grow(c)) {  // overflow: nothing was drawn; larger scratch, record again, re-run
       rt->stats.retries++;
+      rt->learn_caps(po->p);
       int rc = plan_bind_and_record(rt, po);
       if (rc != HSR_OK) return rc;
       e = cudaGraphLaunch(po->exec, rt->stream);
@@ -134,11 +138,10 @@ struct SrvReq {
 };
 
 struct Slot {
-  cudaStream_t stream = nullptr;
-  cudaEvent_t done = nullptr;
-  char* dev = nullptr;
-  size_t dev_cap = 0;
-  char* host = nullptr;
+  cudaStream_t stream = nullptr;  // copies of results, after the batch's kernels
+  cudaEvent_t kdone = nullptr;    // the batch's kernels are done (on the compute stream)
+  cudaEvent_t done = nullptr;     // its results are copied (on the slot's stream)
+  char* host = nullptr;           // the batch's descriptors and control block
   size_t host_cap = 0;
   Plan plan;
   std::vector<hsr_draw_desc> descs;
@@ -157,6 +160,9 @@ struct ServerObj {
   std::deque<SrvReq*> pending;
   std::unordered_map<uint64_t, SrvReq*> reqs;
   std::vector<Slot> slots;
+  cudaStream_t compute = nullptr;  // every batch's launch sequence, in batch order
+  char* dev = nullptr;             // scratch of every batch (they run in turn on `compute`)
+  size_t dev_cap = 0;
   uint64_t pool_used = 0;
   uint64_t next_ticket = 1;
   uint32_t next_batch = 1;
@@ -178,34 +184,51 @@ static size_t req_bytes(const hsr_request& r) {
   return 3 * plane_bytes(r.width, r.height) + (r.shadow_size > 0 ? 3 * plane_bytes(r.shadow_size, r.shadow_size) : 0);
 }
 
-static int slot_reserve(Slot& s, const Plan& p) {
-  if (p.dev_bytes > s.dev_cap) {
-    if (s.dev) cudaFree(s.dev);
-    s.dev = nullptr;
-    s.dev_cap = 0;
-    size_t want = std::max(p.dev_bytes, s.dev_cap + s.dev_cap / 2);
-    if (cudaMalloc(&s.dev, want) != cudaSuccess) { cudaGetLastError(); return HSR_ERR_OUT_OF_MEMORY; }
-    s.dev_cap = want;
+// Grow the scratch and a slot's staging geometrically (x1.5), so a run of slightly larger
+// batches does not reallocate on every batch (each new block of scratch is memory the pool maps
+// while batches run).  Batches run in turn on the compute stream, so
+// one device scratch serves them all (the next batch's counter reset follows the previous
+// batch's control-block read in stream order); it comes from the stream-ordered pool on that
+// stream, so replacing it waits only for the batches before it (cudaMalloc / cudaFree would
+// synchronise the whole device).  Staging stays per slot: the host fills the next batch's
+// descriptors while the previous batch may still be reading its own.
+static int slot_reserve(ServerObj* so, Slot& s, const Plan& p) {
+  if (p.dev_bytes > so->dev_cap) {
+    // headroom over this batch as well: the next batches of a stream are seldom much larger
+    const size_t want = std::max(p.dev_bytes + p.dev_bytes / 2, so->dev_cap + so->dev_cap / 2);
+    if (so->dev) cudaFreeAsync(so->dev, so->compute);
+    so->dev = nullptr;
+    so->dev_cap = 0;
+    if (cudaMallocAsync(reinterpret_cast<void**>(&so->dev), want, so->compute) != cudaSuccess) {
+      cudaGetLastError();
+      so->dev = nullptr;
+      return HSR_ERR_OUT_OF_MEMORY;
+    }
+    so->dev_cap = want;
   }
   if (p.stage_bytes > s.host_cap) {
-    if (s.host) cudaFreeHost(s.host);
+    const size_t want = std::max(p.stage_bytes, s.host_cap + s.host_cap / 2);
+    if (s.host) cudaFreeHost(s.host);  // the slot is idle: nothing in flight reads it
     s.host = nullptr;
     s.host_cap = 0;
-    size_t want = std::max(p.stage_bytes, s.host_cap + s.host_cap / 2);
     if (cudaMallocHost(&s.host, want) != cudaSuccess) { cudaGetLastError(); return HSR_ERR_OUT_OF_MEMORY; }
     s.host_cap = want;
   }
   return HSR_OK;
 }
 
-// Enqueue the slot's plan and the copies of every request's results.
+// Enqueue the slot's plan on the compute stream and the copies of every request's results on
+// the slot's stream after it.
 static int slot_enqueue(ServerObj* so, Slot& s) {
   s.plan.layout();
-  int rc = slot_reserve(s, s.plan);
+  int rc = slot_reserve(so, s, s.plan);
   if (rc != HSR_OK) return rc;
-  s.plan.bind(s.dev, s.host);
-  rc = s.plan.enqueue(s.stream, so->num_sms, so->tuning, nullptr);
+  s.plan.bind(so->dev, s.host);
+  rc = s.plan.enqueue(so->compute, so->num_sms, so->tuning, nullptr);
   if (rc != HSR_OK) return rc;
+  cudaError_t e = cudaEventRecord(s.kdone, so->compute);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(s.stream, s.kdone, 0);
+  if (e != cudaSuccess) return cuda_fail(e, "server: order copies after the batch");
   {
     std::lock_guard<std::mutex> lk(g_mu);
     if (g_rt) g_rt->launches += (uint64_t)s.plan.kernel_count();
@@ -217,7 +240,7 @@ static int slot_enqueue(ServerObj* so, Slot& s) {
     if (q->r.out_depth) cudaMemcpyAsync(q->r.out_depth, base + pl, 4 * n, cudaMemcpyDeviceToHost, s.stream);
     if (q->r.out_prim) cudaMemcpyAsync(q->r.out_prim, base + 2 * pl, 4 * n, cudaMemcpyDeviceToHost, s.stream);
   }
-  cudaError_t e = cudaEventRecord(s.done, s.stream);
+  e = cudaEventRecord(s.done, s.stream);
   return e == cudaSuccess ? HSR_OK : cuda_fail(e, "server: event record");
 }
 
@@ -288,7 +311,7 @@ static bool try_launch(ServerObj* so, Slot& s) {
   const double t = so->now();
   // targets from the stream-ordered pool
   for (SrvReq* q : batch) {
-    if (cudaMallocAsync(reinterpret_cast<void**>(&q->mem), q->bytes, s.stream) != cudaSuccess) {
+    if (cudaMallocAsync(reinterpret_cast<void**>(&q->mem), q->bytes, so->compute) != cudaSuccess) {
       cudaGetLastError();
       q->mem = nullptr;
     }
@@ -348,6 +371,7 @@ static bool try_launch(ServerObj* so, Slot& s) {
   s.busy = true;
   if (rc == HSR_OK) rc = slot_enqueue(so, s);
   if (rc != HSR_OK) {
+    cudaStreamSynchronize(so->compute);
     cudaStreamSynchronize(s.stream);
     finish(so, s, rc);
   }
@@ -358,8 +382,16 @@ static void complete_if_done(ServerObj* so, Slot& s) {
   if (!s.busy || cudaEventQuery(s.done) != cudaSuccess) return;
   const Ctl c = *(const Ctl*)(s.plan.host + s.plan.host_bytes);
   if (s.plan.grow(c)) {  // nothing was drawn: re-run the same batch with larger scratch
+    {
+      std::lock_guard<std::mutex> lk(g_mu);
+      if (g_rt) {
+        g_rt->stats.retries++;
+        g_rt->learn_caps(s.plan);  // later batches start from these capacities
+      }
+    }
     int rc = slot_enqueue(so, s);
     if (rc != HSR_OK) {
+      cudaStreamSynchronize(so->compute);
       cudaStreamSynchronize(s.stream);
       finish(so, s, rc);
     }
@@ -480,13 +512,21 @@ int hsr_server_create(const hsr_server_config* cfg, hsr_server* out) {
     so->tuning = g_rt->tuning;
     so->t0 = std::chrono::steady_clock::now();
     so->slots.resize(cfg->slots);
-    for (Slot& s : so->slots) {
-      if (cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking) != cudaSuccess ||
-          cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming) != cudaSuccess) {
-        cudaGetLastError();
-        delete so;
-        return fail(HSR_ERR_CUDA, "server_create: stream / event creation failed");
+    bool ok = cudaStreamCreateWithFlags(&so->compute, cudaStreamNonBlocking) == cudaSuccess;
+    for (Slot& s : so->slots)
+      ok = ok && cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking) == cudaSuccess &&
+           cudaEventCreateWithFlags(&s.kdone, cudaEventDisableTiming) == cudaSuccess &&
+           cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+      cudaGetLastError();
+      for (Slot& s : so->slots) {
+        if (s.done) cudaEventDestroy(s.done);
+        if (s.kdone) cudaEventDestroy(s.kdone);
+        if (s.stream) cudaStreamDestroy(s.stream);
       }
+      if (so->compute) cudaStreamDestroy(so->compute);
+      delete so;
+      return fail(HSR_ERR_CUDA, "server_create: stream / event creation failed");
     }
     const uint64_t h = g_next_obj++;
     g_servers[h] = so;
@@ -587,13 +627,16 @@ int hsr_server_destroy(hsr_server s) {
   }
   so->cv_work.notify_all();
   if (so->th.joinable()) so->th.join();
+  if (so->dev) cudaFreeAsync(so->dev, so->compute);  // back to the stream-ordered pool
   for (Slot& sl : so->slots) {
     cudaStreamSynchronize(sl.stream);
-    if (sl.dev) cudaFree(sl.dev);
     if (sl.host) cudaFreeHost(sl.host);
     cudaEventDestroy(sl.done);
+    cudaEventDestroy(sl.kdone);
     cudaStreamDestroy(sl.stream);
   }
+  cudaStreamSynchronize(so->compute);
+  cudaStreamDestroy(so->compute);
   for (auto& kv : so->reqs) delete kv.second;
   delete so;
   return HSR_OK;

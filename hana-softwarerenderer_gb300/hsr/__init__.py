@@ -523,8 +523,8 @@ _FLT_MAX = float(np.finfo(np.float32).max)
 
 class Server:
     """Continuous-batching render server (hsr_server_*): requests are queued, admitted while
-    the framebuffer pool has room, batched into launch sequences on `slots` streams, and their
-    colour / depth / prim ids copied into the arrays given at submission."""
+    the framebuffer pool has room, batched into launch sequences (`slots` batches in flight),
+    and their colour / depth / prim ids copied into the arrays given at submission."""
 
     def __init__(self, pool_bytes: int, max_batch: int = 64, slots: int = 2):
         cfg = ServerConfig(pool_bytes, max_batch, slots)

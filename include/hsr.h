@@ -271,15 +271,16 @@ HSR_API int hsr_plan_release(hsr_plan plan);
  * and admitted in arrival order while the framebuffer pool has room for their targets
  * (pool_bytes, memory-based admission; a request larger than the whole pool fails with
  * HSR_ERR_OUT_OF_MEMORY).  Whenever one of the `slots` in-flight batches is free, everything
- * admitted so far (up to max_batch requests) becomes one launch sequence on that slot's
- * stream, so batches overlap on the device.  Colour / depth / prim ids of each request are
+ * admitted so far (up to max_batch requests) becomes one launch sequence; launch sequences
+ * run in turn on the server's compute stream while the next batch is formed and the previous
+ * batch's results are copied out.  Colour / depth / prim ids of each request are
  * copied to the request's host pointers (page-locked memory recommended; NULL skips); the
  * targets return to the pool.  Results equal those of the same request drawn alone. */
 typedef uint64_t hsr_server;
 typedef struct hsr_server_config {
   uint64_t pool_bytes;     /* framebuffer pool budget for targets and shadow maps      */
   int32_t max_batch;       /* requests per launch sequence                              */
-  int32_t slots;           /* launch sequences in flight (streams)                     */
+  int32_t slots;           /* batches in flight (each with its own copy stream)        */
 } hsr_server_config;
 
 typedef struct hsr_request {
