@@ -16,7 +16,9 @@
 //     (gameobject.cpp:12-17); the camera's FOVY 60 degrees, NEAR 0.1, FAR 10000, up (0, 1, 0)
 //     (camera.cpp:11-14); light_vp = orthographic(aspect, 1, 0, 5) * lookat(light, 0, up) and
 //     light_dir = normalize(light - 0) — Camera::get_target_position() returns the origin
-//     (camera.cpp:94-97) — ambient and light colour constants (scene.h:8-9).
+//     (camera.cpp:94-97) — ambient and light colour constants (scene.h:8-9);
+//   - Camera::update_transform (camera.cpp:31-70) with the overloads its calls resolve to:
+//     the float tan / atan2 / acos / sin / cos and the double pow (its 0.95 is a double).
 #include <cmath>
 #include <cstring>
 
@@ -93,6 +95,9 @@ V3 normalize(V3 v) {
   const float f = 1.f / std::sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
   return {v.x * f, v.y * f, v.z * f};
 }
+V3 add(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+V3 scaled(V3 v, float f) { return {v.x * f, v.y * f, v.z * f}; }
+float length(V3 v) { return std::sqrt(v.x * v.x + v.y * v.y + v.z * v.z); }  // Vector3f::normal
 
 constexpr float kPi = 3.1415927f;
 float to_radians(float deg) { return (kPi / 180) * deg; }
@@ -160,6 +165,34 @@ M4 model_matrix(const hsr_transform& t) {
 
 void put(const M4& a, float* out) { std::memcpy(out, &a.m[0][0], sizeof(float) * 16); }
 
+// The camera's field of view, a constant of camera.cpp (FOVY = TO_RADIANS(60)): the reference's
+// tan(FOVY / 2) has a constant argument, which the compiler evaluates at build time.
+const float kFovy = (kPi / 180) * 60;
+
+// calculate_pan (camera.cpp:31-42): the target's move for a pan of the cursor
+V3 camera_pan(V3 from_camera, const hsr_camera_motion& m) {
+  const V3 forward = normalize(from_camera);
+  const V3 left = cross({0.f, 1.f, 0.f}, forward);
+  const V3 up = cross(forward, left);
+  const float distance = length(from_camera);
+  const float factor = distance * std::tan(kFovy / 2) * 2;
+  return add(scaled(scaled(left, m.pan[0]), factor), scaled(scaled(up, m.pan[1]), factor));
+}
+
+// calculate_offset (camera.cpp:44-61): the eye's offset from the target after dolly and orbit
+V3 camera_offset(V3 from_target, const hsr_camera_motion& m) {
+  float radius = length(from_target);
+  float theta = std::atan2(from_target.x, from_target.z);  // azimuth
+  float phi = std::acos(from_target.y / radius);           // polar
+  const float factor = kPi * 2;
+  radius *= (float)std::pow(0.95, (double)m.dolly);
+  theta -= m.orbit[0] * factor;
+  phi -= m.orbit[1] * factor;
+  const float lo = 1e-5f, hi = kPi - 1e-5f;  // clamp (maths.cpp:3-5)
+  phi = phi < lo ? lo : (phi > hi ? hi : phi);
+  return {radius * std::sin(phi) * std::sin(theta), radius * std::cos(phi), radius * std::sin(phi) * std::cos(theta)};
+}
+
 }  // namespace
 
 extern "C" {
@@ -167,6 +200,19 @@ extern "C" {
 int hsr_model_matrix(const hsr_transform* t, float* out) {
   if (!t || !out) return HSR_ERR_INVALID_ARG;
   put(model_matrix(*t), out);
+  return HSR_OK;
+}
+
+int hsr_camera_update(const float position[3], const float target[3], const hsr_camera_motion* motion,
+                      float out_position[3], float out_target[3]) {
+  if (!position || !target || !motion || !out_position || !out_target) return HSR_ERR_INVALID_ARG;
+  const V3 pos = {position[0], position[1], position[2]}, tgt = {target[0], target[1], target[2]};
+  const V3 pan = camera_pan(sub(tgt, pos), *motion);
+  const V3 offset = camera_offset(sub(pos, tgt), *motion);
+  const V3 new_target = add(tgt, pan);
+  const V3 new_position = add(new_target, offset);
+  out_target[0] = new_target.x; out_target[1] = new_target.y; out_target[2] = new_target.z;
+  out_position[0] = new_position.x; out_position[1] = new_position.y; out_position[2] = new_position.z;
   return HSR_OK;
 }
 

@@ -79,6 +79,10 @@ class Transform(ctypes.Structure):
     _fields_ = [("position", ctypes.c_float * 3), ("rotation", ctypes.c_float * 3), ("scale", ctypes.c_float * 3)]
 
 
+class CameraMotion(ctypes.Structure):
+    _fields_ = [("orbit", ctypes.c_float * 2), ("pan", ctypes.c_float * 2), ("dolly", ctypes.c_float)]
+
+
 class SceneParams(ctypes.Structure):
     _fields_ = [("camera_position", ctypes.c_float * 3), ("camera_target", ctypes.c_float * 3),
                 ("light_position", ctypes.c_float * 3), ("width", ctypes.c_int32), ("height", ctypes.c_int32),
@@ -151,6 +155,7 @@ def lib():
         "hsr_shader_data_build": ([ctypes.POINTER(SceneParams), ctypes.c_void_p], ctypes.c_int),
         "hsr_model_matrix": ([ctypes.POINTER(Transform), _f32p], ctypes.c_int),
         "hsr_matrix_invert": ([_f32p, _f32p], ctypes.c_int),
+        "hsr_camera_update": ([_f32p, _f32p, ctypes.POINTER(CameraMotion), _f32p, _f32p], ctypes.c_int),
         "hsr_obj_read": ([ctypes.c_char_p, ctypes.c_uint32, _f32p, _i32p, _f32p, _i32p, _f32p, _i32p, _i32p, _i32p],
                          ctypes.c_int),
         "hsr_tga_read": ([ctypes.c_char_p, ctypes.c_uint32, _u8p, _i32p, _i32p, _i32p], ctypes.c_int),
@@ -289,6 +294,18 @@ def matrix_invert(m) -> np.ndarray:
     out = np.empty(16, np.float32)
     check(lib().hsr_matrix_invert(a.ctypes.data_as(_f32p), out.ctypes.data_as(_f32p)))
     return out
+
+
+def camera_update(position, target, orbit=(0.0, 0.0), pan=(0.0, 0.0), dolly: float = 0.0):
+    """One step of the reference's orbital camera (Camera::update_transform, camera.cpp:63-70):
+    returns the new (position, target) as float32 arrays."""
+    p = np.ascontiguousarray(np.asarray(position, np.float32).reshape(3))
+    t = np.ascontiguousarray(np.asarray(target, np.float32).reshape(3))
+    m = CameraMotion((ctypes.c_float * 2)(*orbit), (ctypes.c_float * 2)(*pan), float(dolly))
+    op, ot = np.empty(3, np.float32), np.empty(3, np.float32)
+    check(lib().hsr_camera_update(p.ctypes.data_as(_f32p), t.ctypes.data_as(_f32p), ctypes.byref(m),
+                                  op.ctypes.data_as(_f32p), ot.ctypes.data_as(_f32p)))
+    return op, ot
 
 
 # ---- asset files (hsr_obj_read / hsr_tga_read / hsr_tga_write; host only, no device) ----

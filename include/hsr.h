@@ -161,6 +161,20 @@ typedef struct hsr_scene_params {
 HSR_API int hsr_shader_data_build(const hsr_scene_params* p, hsr_shader_data* out);
 HSR_API int hsr_model_matrix(const hsr_transform* t, float* out16);       /* GameObject::GetModelMatrix */
 HSR_API int hsr_matrix_invert(const float* m16, float* out16);            /* Matrix4x4::invert          */
+/* One step of the reference's orbital camera, Camera::update_transform (camera.cpp:31-70):
+ * the target moves by the pan (in the camera's left / up plane, scaled by the distance and the
+ * 60-degree field of view), then the eye is placed around the new target from the old offset's
+ * radius, azimuth and polar angle, after dolly (radius * 0.95^dolly) and orbit (angles minus
+ * 2*pi * orbit, polar angle clamped to [1e-5, pi - 1e-5]).  orbit and pan are cursor motions
+ * in window heights and dolly is in scroll steps, accumulated as update_camera does
+ * (camera.cpp:154-177).  Host only, bit for bit with the reference. */
+typedef struct hsr_camera_motion {  /* Motion (camera.h:11) */
+  float orbit[2];
+  float pan[2];
+  float dolly;
+} hsr_camera_motion;
+HSR_API int hsr_camera_update(const float position[3], const float target[3], const hsr_camera_motion* motion,
+                              float out_position[3], float out_target[3]);
 
 /* ---- asset files: Wavefront OBJ (Model::Model, model.cpp:6-48) and TGA
  * (TGAImage::read_tga_file, tgaimage.cpp:40-143).  The readers run on the host and need no

@@ -22,6 +22,7 @@
 //   ref_harness tga    <file.tga> <model_flip> <out.bin>   TGAImage::read_tga_file (+ flip)
 //   ref_harness tgawrite <raw.bin> <rle> <out.tga>      TGAImage::write_tga_file
 //   ref_harness uniforms <params.bin> <out.bin>         model matrix + DrawModel::draw uniforms
+//   ref_harness camera <cases.bin> <out.bin>            Camera::update_transform
 #include "camera.h"
 #include "graphics.h"
 
@@ -380,6 +381,43 @@ int cmd_uniforms(const char* inp, const char* outp) {
   return 0;
 }
 
+// Camera::update_transform (camera.cpp:63-70) for n cases:
+// in = i32 n, then per case f32 position[3], target[3], orbit[2], pan[2], dolly
+// out = per case the new position[3] and target[3]
+// Camera keeps its target private with no getter (get_target_position returns the origin);
+// the class is standard-layout (every member private), so a struct with the same members in
+// the same order reads it.
+struct CameraFields {
+  Vector3f position;
+  Vector3f target;
+  float aspect;
+};
+static_assert(sizeof(CameraFields) == sizeof(Camera), "Camera layout");
+
+int cmd_camera(const char* inp, const char* outp) {
+  Reader r;
+  if (!r.load(inp)) return 2;
+  const int32_t n = r.get<int32_t>();
+  FILE* f = std::fopen(outp, "wb");
+  if (!f) return 2;
+  for (int32_t i = 0; i < n; i++) {
+    Vector3f pos, target;
+    read_vec3(r, pos);
+    read_vec3(r, target);
+    Motion m;
+    m.orbit.x = r.get<float>(); m.orbit.y = r.get<float>();
+    m.pan.x = r.get<float>(); m.pan.y = r.get<float>();
+    m.dolly = r.get<float>();
+    Camera cam(pos, target, 1.f);
+    cam.update_transform(m);
+    const CameraFields* cf = reinterpret_cast<const CameraFields*>(&cam);
+    const float o[6] = {cf->position.x, cf->position.y, cf->position.z, cf->target.x, cf->target.y, cf->target.z};
+    std::fwrite(o, 4, 6, f);
+  }
+  std::fclose(f);
+  return 0;
+}
+
 }  // namespace
 
 // camera.cpp's interactive update_camera reads the Win32 input layer (win32.cpp), which is
@@ -391,12 +429,13 @@ float platform_get_time(void) { return 0.f; }
 
 int main(int argc, char** argv) {
   if (argc >= 4 && std::strcmp(argv[1], "uniforms") == 0) return cmd_uniforms(argv[2], argv[3]);
+  if (argc >= 4 && std::strcmp(argv[1], "camera") == 0) return cmd_camera(argv[2], argv[3]);
   if (argc >= 4 && std::strcmp(argv[1], "obj") == 0) return cmd_obj(argv[2], argv[3]);
   if (argc >= 5 && std::strcmp(argv[1], "tga") == 0) return cmd_tga(argv[2], std::atoi(argv[3]), argv[4]);
   if (argc >= 5 && std::strcmp(argv[1], "tgawrite") == 0) return cmd_tgawrite(argv[2], std::atoi(argv[3]), argv[4]);
   if (argc >= 4 && std::strcmp(argv[1], "draw") == 0) return cmd_draw(argv[2], argv[3], 0);
   if (argc >= 4 && std::strcmp(argv[1], "time") == 0) return cmd_draw(argv[2], nullptr, std::atoi(argv[3]));
   if (argc >= 4 && std::strcmp(argv[1], "mats") == 0) return cmd_mats(argv[2], argv[3]);
-  std::fprintf(stderr, "usage: ref_harness draw|time|mats|obj|tga|tgawrite|uniforms ...\n");
+  std::fprintf(stderr, "usage: ref_harness draw|time|mats|obj|tga|tgawrite|uniforms|camera ...\n");
   return 2;
 }

@@ -210,3 +210,21 @@ def ref_uniforms(position, rotation_deg, scale, eye, target, light, width: int, 
         for n in os.listdir(wd):
             os.unlink(os.path.join(wd, n))
         os.rmdir(wd)
+
+
+def ref_camera(cases: np.ndarray) -> np.ndarray:
+    """Camera::update_transform (camera.cpp:63-70) of the reference for each row of `cases`
+    (position[3], target[3], orbit[2], pan[2], dolly): rows of new position[3], target[3]."""
+    cases = np.ascontiguousarray(cases, np.float32).reshape(-1, 11)
+    wd = tempfile.mkdtemp(prefix="hsrcam_")
+    try:
+        p = os.path.join(wd, "c.bin")
+        o = os.path.join(wd, "o.bin")
+        with open(p, "wb") as f:
+            f.write(struct.pack("<i", len(cases)) + cases.tobytes())
+        subprocess.run([HARNESS, "camera", p, o], check=True)
+        return np.fromfile(o, np.float32).reshape(-1, 6)
+    finally:
+        for n in os.listdir(wd):
+            os.unlink(os.path.join(wd, n))
+        os.rmdir(wd)

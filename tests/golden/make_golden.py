@@ -174,17 +174,54 @@ def matrices(path: str) -> None:
     np.save(path, np.stack(rows).astype(np.float32))
 
 
+def camera_cases(n: int = 200, seed: int = 31) -> np.ndarray:
+    """Inputs of Camera::update_transform: position, target, orbit, pan, dolly.  Random orbits
+    around a target near the origin, plus the edge cases of the reference's formulas: the eye
+    straight above / below the target (azimuth of (0, 0), polar angle clamped), orbits past the
+    poles, no motion, and large dolly steps either way."""
+    rng = np.random.default_rng(seed)
+    pos = rng.normal(0, 1, (n, 3))
+    pos *= rng.uniform(0.3, 6.0, (n, 1)) / np.linalg.norm(pos, axis=1, keepdims=True)
+    target = rng.uniform(-1, 1, (n, 3)) * (rng.random((n, 1)) < 0.7)
+    rows = np.concatenate([pos + target, target, rng.uniform(-0.6, 0.6, (n, 2)), rng.uniform(-0.3, 0.3, (n, 2)),
+                           rng.uniform(-12, 12, (n, 1)).round(0) * (rng.random((n, 1)) < 0.8)], axis=1)
+    special = [
+        [0, 2, 0, 0, 0, 0, 0.1, 0.05, 0.02, -0.01, 1],    # straight above the target
+        [0, -3, 0, 0, 0, 0, -0.2, -0.3, 0, 0, -2],        # straight below
+        [0, 0, 2, 0, 0, 0, 0, 0.9, 0, 0, 0],              # orbit past the north pole (clamped)
+        [0, 0, 2, 0, 0, 0, 0, -0.9, 0, 0, 0],             # past the south pole
+        [1.5, 0.5, -2, 0.25, -0.5, 0.125, 0, 0, 0, 0, 0],  # no motion
+        [0, 0, 2, 0, 0, 0, 0, 0, 0, 0, 40],               # dolly far in
+        [0, 0, 2, 0, 0, 0, 0, 0, 0, 0, -40],              # dolly far out
+        [0.5, 1, 2, 0, 0, 0, 0.25, 0.1, 0.2, -0.15, 3.5],  # fractional dolly
+    ]
+    return np.concatenate([rows, np.array(special, np.float64)]).astype(np.float32)
+
+
+def camera(path: str) -> None:
+    """Camera::update_transform of the reference (camera.cpp:63-70): inputs and outputs."""
+    cases = camera_cases()
+    np.save(path, np.concatenate([cases, refjob.ref_camera(cases)], axis=1).astype(np.float32))
+
+
 def main() -> None:
+    """`make_golden.py` writes every fixture; `make_golden.py frames|matrices|camera ...` only
+    the named groups."""
     if not refjob.build():
         raise SystemExit("reference sources not found; fixtures can only be generated where they exist")
+    want = set(sys.argv[1:]) or {"frames", "matrices", "camera"}
     total = 0
-    for fr in fixtures():
-        p = os.path.join(HERE, fr.name + ".npz")
-        info = save(fr, p)
-        sz = os.path.getsize(p)
-        total += sz
-        print(f"{fr.name:32s} faces={fr.mesh.nfaces:7d} covered={info} {sz/1024:.0f} KiB")
-    matrices(os.path.join(HERE, "matrices.npy"))
+    if "frames" in want:
+        for fr in fixtures():
+            p = os.path.join(HERE, fr.name + ".npz")
+            info = save(fr, p)
+            sz = os.path.getsize(p)
+            total += sz
+            print(f"{fr.name:32s} faces={fr.mesh.nfaces:7d} covered={info} {sz/1024:.0f} KiB")
+    if "matrices" in want:
+        matrices(os.path.join(HERE, "matrices.npy"))
+    if "camera" in want:
+        camera(os.path.join(HERE, "camera_update.npy"))
     print(f"total {total/1024:.0f} KiB")
 
 

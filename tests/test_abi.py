@@ -70,6 +70,7 @@ def test_struct_layouts_match_header(tmp_path):
         "hsr_tuning": (hsr.Tuning, ["bin_factor"]),
         "hsr_transform": (hsr.Transform, ["rotation", "scale"]),
         "hsr_scene_params": (hsr.SceneParams, ["width", "model", "enable_shadow", "gloss", "bump_scale"]),
+        "hsr_camera_motion": (hsr.CameraMotion, ["pan", "dolly"]),
     }
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "hsr.h"', "int main(void) {"]
     for cname, (_, fields) in checks.items():

@@ -1,7 +1,8 @@
-"""CPU: the native uniform builder (hsr_shader_data_build, hsr_model_matrix, hsr_matrix_invert)
-gives the reference's bits — against the golden matrices (generated from the reference's
-maths.cpp), against the Python builder, and, where the reference sources are present, against
-the reference's own GameObject::GetModelMatrix / Camera / DrawModel::draw built headless.
+"""CPU: the native uniform builder (hsr_shader_data_build, hsr_model_matrix, hsr_matrix_invert,
+hsr_camera_update) gives the reference's bits — against the golden matrices and camera steps
+(generated from the reference's maths.cpp and camera.cpp), against the Python builder, and,
+where the reference sources are present, against the reference's own
+GameObject::GetModelMatrix / Camera / DrawModel::draw built headless.
 """
 import os
 
@@ -68,3 +69,37 @@ def test_matches_reference_model_camera_and_light():
                       ("projection_matrix", "proj"), ("light_vp_matrix", "light_vp"),
                       ("camera_vp_matrix", "camera_vp"), ("light_dir", "light_dir")):
             assert np.array_equal(bits(sd[k]), bits(ref[rk])), k
+
+
+def _camera_rows(cases):
+    out = []
+    for r in cases:
+        p, t = hsr.camera_update(r[0:3], r[3:6], r[6:8], r[8:10], r[10])
+        out.append(np.concatenate([p, t]))
+    return np.array(out, np.float32)
+
+
+def test_camera_update_matches_golden_steps():
+    """Camera::update_transform: random orbits, pans and dollies around targets near the origin,
+    the eye straight above and below the target, orbits past either pole (polar angle
+    clamped), no motion, and large dolly steps — every output float bit for bit."""
+    g = np.load(os.path.join(golden_io.GOLDEN, "camera_update.npy"))
+    assert g.shape == (208, 17)
+    assert np.array_equal(bits(_camera_rows(g[:, :11])), bits(g[:, 11:]))
+
+
+def test_camera_update_no_motion_keeps_the_target():
+    p, t = hsr.camera_update((1.5, 0.5, -2.0), (0.25, -0.5, 0.125))
+    assert np.array_equal(bits(t), bits([0.25, -0.5, 0.125]))
+    assert np.allclose(p, [1.5, 0.5, -2.0], atol=1e-5)  # re-derived from radius and angles
+
+
+@needs_ref
+def test_camera_update_matches_reference():
+    import sys
+
+    sys.path.insert(0, golden_io.GOLDEN)
+    import make_golden
+
+    cases = make_golden.camera_cases(300, seed=77)
+    assert np.array_equal(bits(_camera_rows(cases)), bits(refjob.ref_camera(cases)))
