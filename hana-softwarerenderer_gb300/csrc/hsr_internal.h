@@ -5,11 +5,14 @@
 //   k_setup   : per face: fast accept or homogeneous clip (graphics.cpp:132-161), then per
 //               fan triangle divide / cull / viewport / bbox (graphics.cpp:314-347) -> one
 //               64-byte RasterRec, plus per-tile counts (warp-aggregated atomics)
-//   k_scan    : exclusive prefix sum of the per-tile counts (decoupled look-back)
+//   k_scan    : exclusive prefix sums of the per-tile counts and of the non-empty tiles
+//               (decoupled look-back), and the list of non-empty tiles in tile order
 //   k_scatter : (record, tile) pairs into per-tile lists
-//   k_raster  : persistent; one warp owns one screen tile, resolves visibility per pixel
-//               as min over (depth, later-submitted) — the sequential loop's result —
-//               then shades the winners and writes colour / depth / prim id once.
+//   k_clear   : fused clear of the tiles no triangle touches, streamed row by row
+//   k_raster  : persistent over the non-empty tiles; one warp owns one screen tile,
+//               resolves visibility per pixel as min over (depth, later-submitted) — the
+//               sequential loop's result — then shades the winners and writes colour /
+//               depth / prim id once.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -106,12 +109,16 @@ struct __align__(128) DView {
   const uint32_t* sm_color; int32_t smW, smH;
   // this view's work chunks in the batch's chunk spaces (a kernel finds the view of chunk c
   // as the last view whose base is <= c): vertex chunks of kVertexChunk items (its position
-  // chunks, then its normal chunks), setup chunks of kSetupChunk faces
+  // chunks, then its normal chunks), setup chunks of kSetupChunk faces, clear chunks of
+  // kClearChunk pixels (none for a view drawn without the fused clear)
   int32_t vch_base, vch_npos, vch_count;
   int32_t sch_base;
+  int32_t cch_base;
 };
 constexpr int kVertexChunk = 2048;  // positions or normals per vertex-stage chunk
 constexpr int kSetupChunk = 256;    // faces per setup chunk (one per thread of a block)
+constexpr int kClearChunk = 4096;   // pixels per clear chunk (16 per thread of a block)
+constexpr int64_t kMaxBatchTiles = (int64_t)1 << 26;  // tiles of one launch sequence (scan word)
 static_assert(offsetof(DView, prim_base) + sizeof(uint32_t) <= 128, "per-tile fields must share one line");
 
 struct Ctl {
@@ -125,6 +132,8 @@ struct Ctl {
   uint32_t post_next;      // work counter of k_post
   unsigned long long shaded_px;  // pixels whose winner was shaded by the raster
   unsigned long long frag_px;    // covered (pixel, triangle) pairs the raster depth-tested
+  uint32_t ne_tiles;             // tiles with at least one record (k_scan)
+  uint32_t ctl_pad;
 };
 
 // A triangle whose bounding box touches more than kMaxRecordTiles tiles, queued by setup
@@ -154,6 +163,8 @@ struct Scratch {
   uint32_t* tile_count;     // [ntiles]
   uint32_t* tile_fill;      // [ntiles]
   uint32_t* tile_off;       // [ntiles]
+  uint32_t* ne_off;         // [ntiles + 1] non-empty tiles before each tile
+  uint32_t* tile_list;      // [ntiles] the non-empty tiles in tile order (ne_tiles of them)
   unsigned long long* scan_status;  // [scan blocks]
   uint32_t* bins;   uint32_t bin_cap;
   int32_t ntiles;
@@ -168,6 +179,7 @@ int launch_post(const DView* views, int tile, Scratch sc, int grid, cudaStream_t
 int launch_big(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s);
 int launch_scan(Scratch sc, cudaStream_t s);
 int launch_scatter(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s);
+int launch_clear_empty(const DView* views, int tile, int nchunks, Scratch sc, int grid, cudaStream_t s);
 int launch_raster(const DView* views, int tile, Scratch sc, int grid, int warps, cudaStream_t s);
 int scan_blocks(int ntiles);
 

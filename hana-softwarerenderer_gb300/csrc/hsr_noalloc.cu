@@ -115,7 +115,9 @@ static int noalloc_draw(Runtime* rt, const hsr_draw_desc& d) {
   v.vch_npos = (m->npos + kVertexChunk - 1) / kVertexChunk;
   v.vch_count = v.vch_npos + (wnrm ? (m->nnrm + kVertexChunk - 1) / kVertexChunk : 0);
   v.sch_base = 0;
+  v.cch_base = 0;
   const int nvch = v.vch_count;
+  const int ncch = (d.flags & HSR_DRAW_CLEAR) ? (int)(((size_t)tg->w * (size_t)tg->h + kClearChunk - 1) / kClearChunk) : 0;
   const int nsch = (m->nfaces + kSetupChunk - 1) / kSetupChunk;
   const size_t faces = (size_t)m->nfaces, tiles = (size_t)v.ntiles;
   const size_t rec_cap = faces + faces / 4 + 1024, clip_cap = faces / 16 + 256, big_cap = faces / 64 + 256;
@@ -135,6 +137,8 @@ static int noalloc_draw(Runtime* rt, const hsr_draw_desc& d) {
   const size_t o_stat = off; off = nal(off + sizeof(unsigned long long) * (size_t)std::max(nscan, 1));
   const size_t zero_bytes = off - o_zero;
   const size_t o_toff = off; off = nal(off + sizeof(uint32_t) * tiles);
+  const size_t o_neoff = off; off = nal(off + sizeof(uint32_t) * (tiles + 1));
+  const size_t o_list = off; off = nal(off + sizeof(uint32_t) * tiles);
   const size_t o_recs = off; off = nal(off + sizeof(RasterRec) * rec_cap);
   const size_t o_pay = off; off = nal(off + sizeof(Payload) * rec_cap);
   const size_t o_clipq = off; off = nal(off + sizeof(int2) * clip_cap);
@@ -161,6 +165,8 @@ static int noalloc_draw(Runtime* rt, const hsr_draw_desc& d) {
   sc.tile_count = (uint32_t*)(dev + o_cnt);
   sc.tile_fill = (uint32_t*)(dev + o_fill);
   sc.tile_off = (uint32_t*)(dev + o_toff);
+  sc.ne_off = (uint32_t*)(dev + o_neoff);
+  sc.tile_list = (uint32_t*)(dev + o_list);
   sc.scan_status = (unsigned long long*)(dev + o_stat);
   sc.bins = (uint32_t*)(dev + o_bins); sc.bin_cap = (uint32_t)bin_cap;
   sc.ntiles = (int32_t)tiles;
@@ -180,9 +186,10 @@ static int noalloc_draw(Runtime* rt, const hsr_draw_desc& d) {
   if (!kr) kr = launch_big(dview, T, sc, rt->num_sms * 2, s);
   if (!kr) kr = launch_scan(sc, s);
   if (!kr) kr = launch_scatter(dview, T, sc, (int)std::max<size_t>((rec_cap + 255) / 256, 1), s);
+  if (!kr) kr = launch_clear_empty(dview, T, ncch, sc, rt->num_sms * 8, s);
   if (!kr) kr = launch_raster(dview, T, sc, rt->num_sms * rt->tuning.ctas_per_sm, rt->tuning.warps_per_cta, s);
   if (kr) return cuda_fail((cudaError_t)kr, "draw_noalloc: kernel launch");
-  rt->launches += 8;
+  rt->launches += ncch ? 9 : 8;
   Ctl* hc = reinterpret_cast<Ctl*>(h + host_bytes);
   e = cudaMemcpyAsync(hc, sc.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);

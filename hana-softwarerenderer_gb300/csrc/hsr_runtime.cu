@@ -243,14 +243,17 @@ int Runtime::plan_build(const hsr_draw_desc* descs, int n, Plan& p) {
     v.vch_npos = (m->npos + kVertexChunk - 1) / kVertexChunk;
     v.vch_count = v.vch_npos + (shader_needs_wnrm(d.shader) ? (m->nnrm + kVertexChunk - 1) / kVertexChunk : 0);
     v.sch_base = p.nsch;
+    v.cch_base = p.ncch;
     p.nvch += v.vch_count;
     p.nsch += (m->nfaces + kSetupChunk - 1) / kSetupChunk;
+    if (d.flags & HSR_DRAW_CLEAR) p.ncch += (int)(((size_t)tg->w * (size_t)tg->h + kClearChunk - 1) / kClearChunk);
   }
   for (int k = 0; k < n; k++) {
     if (p.views[k].dep0 >= 0) p.views[p.views[k].dep0].has_dependents = 1;
     if (p.views[k].dep1 >= 0) p.views[p.views[k].dep1].has_dependents = 1;
   }
-  if (p.total_tiles > (size_t)INT32_MAX) return fail(HSR_ERR_INVALID_ARG, "draw batch: too many tiles");
+  if (p.total_tiles >= (size_t)kMaxBatchTiles)
+    return fail(HSR_ERR_INVALID_ARG, "draw batch: too many tiles for one launch sequence (2^26)");
   p.view_bytes = bytes;
   p.rec_cap = std::max<size_t>(cap_rec_hint, p.total_faces + p.total_faces / 4 + 1024);
   p.clip_cap = std::max<size_t>(cap_clip_hint, p.total_faces / 16 + 256);
@@ -267,7 +270,7 @@ void Plan::layout() {
   bin_cap = std::min<size_t>(bin_cap, 0xfffff000u);
   nscan = scan_blocks((int)total_tiles);
   // [views | chunks | per-view vertex outputs | ctl | view_done | tile_count | tile_fill |
-  //  scan_status | tile_off | recs | clipbuf | bins]; the zeroed part is one memset
+  //  scan_status | tile_off | ne_off | tile_list | recs | clipbuf | bins]; the zeroed part is one memset
   size_t off = 0;
   o_views = off; off = align_up(off + sizeof(DView) * n, 256);
   host_bytes = off;
@@ -280,6 +283,8 @@ void Plan::layout() {
   o_stat = off; off = align_up(off + sizeof(unsigned long long) * std::max(nscan, 1), 256);
   zero_bytes = off - o_zero;
   o_toff = off; off = align_up(off + sizeof(uint32_t) * total_tiles, 256);
+  o_neoff = off; off = align_up(off + sizeof(uint32_t) * (total_tiles + 1), 256);
+  o_list = off; off = align_up(off + sizeof(uint32_t) * total_tiles, 256);
   o_recs = off; off = align_up(off + sizeof(RasterRec) * rec_cap, 256);
   o_pay = off; off = align_up(off + sizeof(Payload) * rec_cap, 256);
   o_clip = off; off = align_up(off + sizeof(int2) * clip_cap, 256);
@@ -308,13 +313,15 @@ void Plan::bind(char* dev_base, char* host_base) {
   sc.tile_count = (uint32_t*)(dev + o_cnt);
   sc.tile_fill = (uint32_t*)(dev + o_fill);
   sc.tile_off = (uint32_t*)(dev + o_toff);
+  sc.ne_off = (uint32_t*)(dev + o_neoff);
+  sc.tile_list = (uint32_t*)(dev + o_list);
   sc.scan_status = (unsigned long long*)(dev + o_stat);
   sc.bins = (uint32_t*)(dev + o_bins); sc.bin_cap = (uint32_t)bin_cap;
   sc.ntiles = (int32_t)total_tiles;
   sc.nviews = n;
 }
 
-// Upload of the view descriptors, one memset, five kernels, read-back of the control
+// Upload of the view descriptors, one memset, the kernels, read-back of the control
 // block: everything stream-ordered, nothing synchronous (capturable into a CUDA graph).
 int Plan::enqueue(cudaStream_t s, int num_sms, const hsr_tuning& tu, cudaEvent_t* ev) {
   const DView* dviews = (const DView*)(dev + o_views);
@@ -344,6 +351,8 @@ int Plan::enqueue(cudaStream_t s, int num_sms, const hsr_tuning& tu, cudaEvent_t
   kr = launch_scatter(dviews, tile, sc, (int)std::max<size_t>(std::min<size_t>((rec_cap + 255) / 256, (size_t)num_sms * 8), 1), s);
   if (kr) return cuda_fail((cudaError_t)kr, "scatter kernel");
   if (ev && ev[5]) cudaEventRecord(ev[5], s);
+  kr = launch_clear_empty(dviews, tile, ncch, sc, num_sms * 8, s);
+  if (kr) return cuda_fail((cudaError_t)kr, "clear kernel");
   kr = launch_raster(dviews, tile, sc, num_sms * tu.ctas_per_sm, tu.warps_per_cta, s);
   if (kr) return cuda_fail((cudaError_t)kr, "raster kernel");
   if (ev) cudaEventRecord(ev[6], s);
@@ -353,7 +362,7 @@ int Plan::enqueue(cudaStream_t s, int num_sms, const hsr_tuning& tu, cudaEvent_t
 }
 
 int Plan::kernel_count() const {
-  return (nvch ? 1 : 0) + (nsch ? 1 : 0) + 3 + (nscan > 0 ? 1 : 0) + 2;
+  return (nvch ? 1 : 0) + (nsch ? 1 : 0) + 3 + (nscan > 0 ? 1 : 0) + (ncch ? 1 : 0) + 2;
 }
 
 // Grow the capacity an overflow reported; returns false if nothing overflowed.

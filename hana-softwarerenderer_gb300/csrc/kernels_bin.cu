@@ -2,11 +2,13 @@
 // each triangle's bounding box (graphics.cpp:349-375).  Here the (record, tile) pairs are
 // laid out per tile so that one warp can own a tile in the raster.
 //
-// k_scan    exclusive prefix sum of per-tile counts, single pass with decoupled look-back;
+// k_scan    exclusive prefix sums of the per-tile counts and of the non-empty tiles, single
+//           pass with decoupled look-back, and the list of non-empty tiles in tile order;
 //           block order comes from a ticket so a block only waits on blocks that already
 //           run, and every wait is bounded (error bit + give up, never a hang).
 // k_scatter writes record indices into the per-tile lists with warp-aggregated atomics;
 //           a record touches at most kMaxRecordTiles tiles (setup splits larger ones).
+// k_clear_empty  the fused clear of the tiles no record touches, streamed in row order.
 #include "hsr_device.cuh"
 
 namespace hsr {
@@ -27,36 +29,49 @@ __device__ __forceinline__ unsigned long long ld_volatile64(const unsigned long 
   return *reinterpret_cast<const volatile unsigned long long*>(p);
 }
 
+// Scan word: bits 0-35 the count prefix, bits 36-61 the non-empty tile prefix, 62-63 the
+// look-back flags.  Neither field can carry into the next: a batch has fewer than 2^26
+// tiles (kMaxBatchTiles), and 2^36 (record, tile) pairs would need more records than the
+// device memory holds (each record touches at most kMaxRecordTiles tiles).
+constexpr int kCntBits = 36;
+constexpr unsigned long long kCntMask = (1ull << kCntBits) - 1;
+constexpr unsigned long long kOneTile = 1ull << kCntBits;
+
+__device__ __forceinline__ unsigned long long scan_item(uint32_t count) {
+  return (unsigned long long)count + (count ? kOneTile : 0ull);
+}
+
 __global__ void __launch_bounds__(kScanThreads) k_scan(Scratch sc) {
-  __shared__ uint32_t warp_sums[kScanThreads / 32];
-  __shared__ uint32_t s_block, s_prefix;
+  __shared__ unsigned long long warp_sums[kScanThreads / 32];
+  __shared__ unsigned long long s_prefix;
+  __shared__ uint32_t s_block;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (threadIdx.x == 0) s_block = atomicAdd(&sc.ctl->scan_ticket, 1u);
   __syncthreads();
   const uint32_t blk = s_block;
   const int base = (int)blk * kScanTile + (int)threadIdx.x * kScanItems;
   uint32_t vals[kScanItems];
-  uint32_t local = 0;
+  unsigned long long local = 0;
 #pragma unroll
   for (int k = 0; k < kScanItems; k++) {
     vals[k] = (base + k < sc.ntiles) ? sc.tile_count[base + k] : 0u;
-    local += vals[k];
+    local += scan_item(vals[k]);
   }
   // block-wide exclusive scan of the thread sums
-  uint32_t incl = local;
+  unsigned long long incl = local;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    uint32_t y = __shfl_up_sync(kFull, incl, o);
+    const unsigned long long y = __shfl_up_sync(kFull, incl, o);
     if (lane >= o) incl += y;
   }
   if (lane == 31) warp_sums[warp] = incl;
   __syncthreads();
   if (warp == 0) {
-    uint32_t w = lane < kScanThreads / 32 ? warp_sums[lane] : 0u;
-    uint32_t wi = w;
+    const unsigned long long w = lane < kScanThreads / 32 ? warp_sums[lane] : 0ull;
+    unsigned long long wi = w;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      uint32_t y = __shfl_up_sync(kFull, wi, o);
+      const unsigned long long y = __shfl_up_sync(kFull, wi, o);
       if (lane >= o) wi += y;
     }
     if (lane < kScanThreads / 32) warp_sums[lane] = wi - w;  // exclusive per warp
@@ -64,7 +79,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Scratch sc) {
       // lane 7 holds the block aggregate; publish and look back
       const unsigned long long agg = wi;
       unsigned long long* st = sc.scan_status;
-      uint32_t prefix = 0;
+      unsigned long long prefix = 0;
       if (blk == 0) {
         atomicExch(&st[0], kFlagPre | agg);
       } else {
@@ -73,7 +88,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Scratch sc) {
         int p = (int)blk - 1;
         long spins = 0;
         while (p >= 0) {
-          unsigned long long s = ld_volatile64(&st[p]);
+          const unsigned long long s = ld_volatile64(&st[p]);
           if ((s >> 62) == 0) {
             if (++spins > kSpinLimit) {
               atomicOr(&sc.ctl->error, kErrScanTimeout);
@@ -86,23 +101,33 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Scratch sc) {
           if ((s >> 62) == 2) break;
           p--;
         }
-        prefix = (uint32_t)acc;
+        prefix = acc;
         atomicExch(&st[blk], kFlagPre | (acc + agg));
       }
       s_prefix = prefix;
       if ((int)blk == scan_blocks_hd(sc.ntiles) - 1) {
-        const uint32_t total = prefix + (uint32_t)agg;
-        sc.ctl->bin_total = total;
-        if (total > sc.bin_cap) atomicOr(&sc.ctl->error, kErrBinOverflow);
+        const unsigned long long total = prefix + agg;
+        const unsigned long long pairs = total & kCntMask;
+        const uint32_t ne = (uint32_t)(total >> kCntBits);
+        sc.ctl->bin_total = (uint32_t)min(pairs, 0xffffffffull);
+        if (pairs > sc.bin_cap) atomicOr(&sc.ctl->error, kErrBinOverflow);
+        sc.ctl->ne_tiles = ne;
+        sc.ne_off[sc.ntiles] = ne;
       }
     }
   }
   __syncthreads();
-  uint32_t run = s_prefix + warp_sums[warp] + (incl - local);
+  unsigned long long run = s_prefix + warp_sums[warp] + (incl - local);
 #pragma unroll
   for (int k = 0; k < kScanItems; k++) {
-    if (base + k < sc.ntiles) sc.tile_off[base + k] = run;
-    run += vals[k];
+    const int t = base + k;
+    if (t < sc.ntiles) {
+      const uint32_t ne = (uint32_t)(run >> kCntBits);
+      sc.tile_off[t] = (uint32_t)(run & kCntMask);  // below bin_cap unless the batch overflows
+      sc.ne_off[t] = ne;
+      if (vals[k]) sc.tile_list[ne] = (uint32_t)t;
+    }
+    run += scan_item(vals[k]);
   }
 }
 
@@ -157,6 +182,58 @@ __global__ void __launch_bounds__(256) k_scatter(const DView* __restrict__ views
 
 int launch_scatter(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s) {
   k_scatter<<<grid, 256, 0, s>>>(views, tile, sc);
+  return (int)cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------
+// The fused clear (renderbuffer_clear_color / renderbuffer_clear_depth, renderbuffer.cpp:59-75,
+// prim ids -> 0) of the pixels whose tile holds no record: the raster visits only the
+// non-empty tiles and writes every pixel of those.  A chunk is kClearChunk consecutive pixels
+// of one view in row-major order, so a warp's stores form one contiguous run per plane; the
+// pixel's tile count (the same word for up to T neighbours) decides whether it is written.
+__global__ void __launch_bounds__(256) k_clear_empty(const DView* __restrict__ views, int T, int nchunks, Scratch sc) {
+  __shared__ int32_t s_cbase[kSharedViews];
+  const int nv = sc.nviews;
+  const bool in_shared = nv <= kSharedViews;
+  if (in_shared)
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) s_cbase[i] = views[i].cch_base;
+  __syncthreads();
+  if (sc.ctl->error & kErrCapacity) return;  // an overflowing sequence draws nothing
+  const int ts = __ffs(T) - 1;
+  for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    // the view of chunk c: the last view whose base is <= c (views without chunks share
+    // their successor's base and are never the last such view)
+    int lo = 0, hi = nv - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if ((in_shared ? s_cbase[mid] : views[mid].cch_base) <= c) lo = mid; else hi = mid - 1;
+    }
+    const DView& v = views[lo];
+    const int W = v.W, npx = v.W * v.H;  // below 2^30 (targets are at most 32768 x 32768)
+    const int i0 = (c - v.cch_base) * kClearChunk + (int)threadIdx.x;
+    const int i1 = min((c - v.cch_base + 1) * kClearChunk, npx);
+    int y = i0 / W, x = i0 - y * W;
+    const int qy = 256 / W, qx = 256 - qy * W;  // the step of 256 pixels in rows and columns
+    const uint32_t rgba = v.clear_rgba;
+    const float depth = v.clear_depth;
+    const int32_t tb = v.tile_base, tx = v.tiles_x;
+    for (int i = i0; i < i1; i += 256) {
+      if (sc.tile_count[tb + (y >> ts) * tx + (x >> ts)] == 0u) {
+        v.color[i] = rgba;
+        v.depth[i] = depth;
+        if (v.prim) v.prim[i] = 0u;
+      }
+      x += qx;
+      y += qy;
+      if (x >= W) { x -= W; y++; }
+    }
+  }
+}
+
+int launch_clear_empty(const DView* views, int tile, int nchunks, Scratch sc, int grid, cudaStream_t s) {
+  if (nchunks <= 0) return 0;
+  const int blocks = grid < nchunks ? (grid > 0 ? grid : 1) : nchunks;
+  k_clear_empty<<<blocks, 256, 0, s>>>(views, tile, nchunks, sc);
   return (int)cudaGetLastError();
 }
 

@@ -42,9 +42,12 @@ __device__ __forceinline__ int find_view(const DView* views, const int32_t* tbas
   return lo;
 }
 
+// Wait until every non-empty tile of view `dep` is done (its empty tiles were cleared by
+// k_clear_empty, which runs before the raster).
 __device__ __forceinline__ void wait_view(const Scratch& sc, const DView* views, int dep) {
   if (dep < 0) return;
-  const uint32_t need = (uint32_t)views[dep].ntiles;
+  const int tb = views[dep].tile_base;
+  const uint32_t need = sc.ne_off[tb + views[dep].ntiles] - sc.ne_off[tb];
   long spins = 0;
   while (*reinterpret_cast<volatile uint32_t*>(&sc.view_done[dep]) < need) {
     if (++spins > kWaitLimit) {
@@ -157,7 +160,8 @@ __device__ __forceinline__ uint32_t shade_tile(const DView& v, const Scratch& sc
   return shaded;
 }
 
-// One warp per screen tile.  For each batch of 32 records of the tile list, every record's
+// One warp per non-empty screen tile (k_scan lists them in tile order; k_clear_empty has
+// written the others).  For each batch of 32 records of the tile list, every record's
 // bounding-box pixels inside the tile form a run of candidates; the non-empty runs are
 // compacted and laid end to end (warp prefix sum) and the lanes walk the candidates 32 at
 // a time, so the work is proportional to the pixels the triangles can touch rather than
@@ -189,26 +193,32 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
   if (sc.ctl->error & kErrCapacity) return;
   const uint32_t nrec = min(sc.ctl->rec_count, sc.rec_cap);
 
-  // Tiles are handed out by one counter, two ahead: while a tile is rasterised, the next
-  // tile's list bounds are already loading and the one after it is being claimed, so neither
-  // the counter's round trip nor the list lookup waits on the critical path (dependencies
-  // only point to lower tile indices, so holding later tiles never blocks).
+  // The non-empty tiles are handed out by one counter over their list, two ahead: while a
+  // tile is rasterised, the next tile's list bounds are already loading and the one after it
+  // is being claimed, so neither the counter's round trip nor the list lookup waits on the
+  // critical path (the list is in tile order and dependencies only point to lower tile
+  // indices, so holding later tiles never blocks).
+  const uint32_t nlist = min(sc.ctl->ne_tiles, (uint32_t)sc.ntiles);
   const uint32_t ntiles = (uint32_t)sc.ntiles;
-  uint32_t t = 0, t_ahead = 0;
+  uint32_t li = 0, li_ahead = 0;  // positions in the list
   if (lane == 0) {
-    t = atomicAdd(&sc.ctl->tile_next, 1u);
-    t_ahead = atomicAdd(&sc.ctl->tile_next, 1u);
+    li = atomicAdd(&sc.ctl->tile_next, 1u);
+    li_ahead = atomicAdd(&sc.ctl->tile_next, 1u);
   }
-  t = __shfl_sync(kFull, t, 0);
+  li = __shfl_sync(kFull, li, 0);
+  uint32_t t = li < nlist ? sc.tile_list[li] : ntiles;
   uint32_t n = 0, off = 0;
   if (t < ntiles) {
     n = sc.tile_count[t];
     off = sc.tile_off[t];
   }
+  // views of a warp's tiles only move forward: after the first, search on from the last one
+  int vi = t < ntiles ? find_view(views, tbase, sc.nviews, (int)t) : 0;
   for (;;) {
     if (t >= ntiles) break;
-    const uint32_t t_next = __shfl_sync(kFull, t_ahead, 0);
-    if (lane == 0) t_ahead = t_next < ntiles ? atomicAdd(&sc.ctl->tile_next, 1u) : ntiles;
+    const uint32_t li_next = __shfl_sync(kFull, li_ahead, 0);
+    if (lane == 0) li_ahead = li_next < nlist ? atomicAdd(&sc.ctl->tile_next, 1u) : nlist;
+    const uint32_t t_next = li_next < nlist ? sc.tile_list[li_next] : ntiles;
     uint32_t n_next = 0, off_next = 0;
     if (t_next < ntiles) {
       n_next = sc.tile_count[t_next];
@@ -218,7 +228,11 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
       const DView* vn = views + find_view(views, tbase, sc.nviews, (int)t_next);
       asm volatile("prefetch.global.L1 [%0];" ::"l"(vn));
     }
-    const int vi = find_view(views, tbase, sc.nviews, (int)t);
+    if (tbase) {
+      while (vi + 1 < sc.nviews && tbase[vi + 1] <= (int)t) vi++;
+    } else {
+      vi = find_view(views, tbase, sc.nviews, (int)t);
+    }
     const DView& v = views[vi];
     if (lane == 0) {
       wait_view(sc, views, v.dep0);
@@ -230,21 +244,7 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
     const int ox = tx * T, oy = ty * T;
     const bool clear = (v.flags & HSR_DRAW_CLEAR) != 0u;
 
-    if (n == 0) {
-      if (clear) {
-#pragma unroll
-        for (int q = 0; q < PPL; q++) {
-          const int p = lane + 32 * q;
-          const int x = ox + p % T, y = oy + p / T;
-          if (x < v.W && y < v.H) {
-            const size_t idx = (size_t)y * v.W + x;
-            v.color[idx] = v.clear_rgba;
-            v.depth[idx] = v.clear_depth;
-            if (v.prim) v.prim[idx] = 0u;
-          }
-        }
-      }
-    } else {
+    if (n != 0) {  // always: the list holds the tiles with records
 #pragma unroll
       for (int q = 0; q < PPL; q++) {
         const int p = lane + 32 * q;
