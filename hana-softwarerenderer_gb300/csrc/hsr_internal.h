@@ -7,8 +7,8 @@
 //               64-byte RasterRec, plus per-tile counts (warp-aggregated atomics)
 //   k_scan    : exclusive prefix sums of the per-tile counts and of the non-empty tiles
 //               (decoupled look-back), and the list of non-empty tiles in tile order
-//   k_scatter : (record, tile) pairs into per-tile lists
-//   k_clear   : fused clear of the tiles no triangle touches, streamed row by row
+//   k_scatter : (record, tile) pairs into per-tile lists; beside it, in the same grid, the
+//               fused clear of the tiles no triangle touches, streamed row by row
 //   k_raster  : persistent over the non-empty tiles; one warp owns one screen tile,
 //               resolves visibility per pixel as min over (depth, later-submitted) — the
 //               sequential loop's result — then shades the winners and writes colour /
@@ -178,8 +178,7 @@ int launch_emit(const DView* views, int tile, Scratch sc, int grid, cudaStream_t
 int launch_post(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s);
 int launch_big(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s);
 int launch_scan(Scratch sc, cudaStream_t s);
-int launch_scatter(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s);
-int launch_clear_empty(const DView* views, int tile, int nchunks, Scratch sc, int grid, cudaStream_t s);
+int launch_scatter(const DView* views, int tile, Scratch sc, int grid, int clear_chunks, cudaStream_t s);
 int launch_raster(const DView* views, int tile, Scratch sc, int grid, int warps, cudaStream_t s);
 int scan_blocks(int ntiles);
 

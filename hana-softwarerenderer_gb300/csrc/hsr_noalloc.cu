@@ -185,11 +185,10 @@ static int noalloc_draw(Runtime* rt, const hsr_draw_desc& d) {
   if (!kr) kr = launch_post(dview, T, sc, rt->num_sms * 4, s);
   if (!kr) kr = launch_big(dview, T, sc, rt->num_sms * 2, s);
   if (!kr) kr = launch_scan(sc, s);
-  if (!kr) kr = launch_scatter(dview, T, sc, (int)std::max<size_t>((rec_cap + 255) / 256, 1), s);
-  if (!kr) kr = launch_clear_empty(dview, T, ncch, sc, rt->num_sms * 8, s);
+  if (!kr) kr = launch_scatter(dview, T, sc, rt->num_sms * 8, ncch, s);
   if (!kr) kr = launch_raster(dview, T, sc, rt->num_sms * rt->tuning.ctas_per_sm, rt->tuning.warps_per_cta, s);
   if (kr) return cuda_fail((cudaError_t)kr, "draw_noalloc: kernel launch");
-  rt->launches += ncch ? 9 : 8;
+  rt->launches += 8;
   Ctl* hc = reinterpret_cast<Ctl*>(h + host_bytes);
   e = cudaMemcpyAsync(hc, sc.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);

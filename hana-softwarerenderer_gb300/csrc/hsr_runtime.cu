@@ -348,11 +348,11 @@ int Plan::enqueue(cudaStream_t s, int num_sms, const hsr_tuning& tu, cudaEvent_t
   if (ev && ev[4]) cudaEventRecord(ev[4], s);
   // grid-stride over the records: a full-occupancy grid, not one sized by the capacity
   // (which can be far above this batch's record count)
-  kr = launch_scatter(dviews, tile, sc, (int)std::max<size_t>(std::min<size_t>((rec_cap + 255) / 256, (size_t)num_sms * 8), 1), s);
+  // one full wave of 256-thread blocks (fewer when there are few records and nothing to clear)
+  const size_t want = ncch ? (size_t)num_sms * 8 : std::min<size_t>((rec_cap + 255) / 256, (size_t)num_sms * 8);
+  kr = launch_scatter(dviews, tile, sc, (int)std::max<size_t>(want, 1), ncch, s);
   if (kr) return cuda_fail((cudaError_t)kr, "scatter kernel");
   if (ev && ev[5]) cudaEventRecord(ev[5], s);
-  kr = launch_clear_empty(dviews, tile, ncch, sc, num_sms * 8, s);
-  if (kr) return cuda_fail((cudaError_t)kr, "clear kernel");
   kr = launch_raster(dviews, tile, sc, num_sms * tu.ctas_per_sm, tu.warps_per_cta, s);
   if (kr) return cuda_fail((cudaError_t)kr, "raster kernel");
   if (ev) cudaEventRecord(ev[6], s);
@@ -362,7 +362,7 @@ int Plan::enqueue(cudaStream_t s, int num_sms, const hsr_tuning& tu, cudaEvent_t
 }
 
 int Plan::kernel_count() const {
-  return (nvch ? 1 : 0) + (nsch ? 1 : 0) + 3 + (nscan > 0 ? 1 : 0) + (ncch ? 1 : 0) + 2;
+  return (nvch ? 1 : 0) + (nsch ? 1 : 0) + 3 + (nscan > 0 ? 1 : 0) + 2;
 }
 
 // Grow the capacity an overflow reported; returns false if nothing overflowed.

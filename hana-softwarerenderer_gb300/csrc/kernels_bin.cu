@@ -8,7 +8,7 @@
 //           run, and every wait is bounded (error bit + give up, never a hang).
 // k_scatter writes record indices into the per-tile lists with warp-aggregated atomics;
 //           a record touches at most kMaxRecordTiles tiles (setup splits larger ones).
-// k_clear_empty  the fused clear of the tiles no record touches, streamed in row order.
+//           The same grid clears the tiles no record touches, streamed in row order.
 #include "hsr_device.cuh"
 
 namespace hsr {
@@ -139,14 +139,17 @@ int launch_scan(Scratch sc, cudaStream_t s) {
 }
 
 // ---------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_scatter(const DView* __restrict__ views, int T, Scratch sc) {
+// (record, tile) pairs into the per-tile lists, records [first block's, nrec) in steps of
+// `nblocks` blocks.
+__device__ __forceinline__ void scatter_records(const DView* __restrict__ views, int T, const Scratch& sc, uint32_t block,
+                                                uint32_t nblocks) {
   const int lane = threadIdx.x & 31;
   const uint32_t nrec = min(sc.ctl->rec_count, sc.rec_cap);
   if (sc.ctl->error & (kErrBinOverflow | kErrRecOverflow | kErrClipOverflow | kErrScanTimeout)) return;
-  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t stride = nblocks * blockDim.x;
   const int ts = __ffs(T) - 1;  // T is a power of two
   // warp-uniform trip count so every lane takes part in the warp-level collectives
-  for (uint32_t i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < nrec; i0 += stride) {
+  for (uint32_t i0 = block * blockDim.x + (threadIdx.x & ~31u); i0 < nrec; i0 += stride) {
     const uint32_t i = i0 + (uint32_t)lane;
     const bool ok = i < nrec;
     int tx0 = 0, ty0 = 0, ntw = 0, nt = 0, tbase = 0, tiles_x = 0;
@@ -180,33 +183,25 @@ __global__ void __launch_bounds__(256) k_scatter(const DView* __restrict__ views
   }
 }
 
-int launch_scatter(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s) {
-  k_scatter<<<grid, 256, 0, s>>>(views, tile, sc);
-  return (int)cudaGetLastError();
-}
-
-// ---------------------------------------------------------------------------------------
 // The fused clear (renderbuffer_clear_color / renderbuffer_clear_depth, renderbuffer.cpp:59-75,
 // prim ids -> 0) of the pixels whose tile holds no record: the raster visits only the
 // non-empty tiles and writes every pixel of those.  A chunk is kClearChunk consecutive pixels
 // of one view in row-major order, so a warp's stores form one contiguous run per plane; the
 // pixel's tile count (the same word for up to T neighbours) decides whether it is written.
-__global__ void __launch_bounds__(256) k_clear_empty(const DView* __restrict__ views, int T, int nchunks, Scratch sc) {
-  __shared__ int32_t s_cbase[kSharedViews];
-  const int nv = sc.nviews;
-  const bool in_shared = nv <= kSharedViews;
-  if (in_shared)
-    for (int i = threadIdx.x; i < nv; i += blockDim.x) s_cbase[i] = views[i].cch_base;
-  __syncthreads();
+// Chunks [block, nchunks) in steps of `nblocks`; `cbase` holds the views' chunk bases when
+// the batch has at most kSharedViews views (else null).
+__device__ __forceinline__ void clear_empty_tiles(const DView* __restrict__ views, int T, int nchunks, const Scratch& sc,
+                                                  int block, int nblocks, const int32_t* cbase) {
   if (sc.ctl->error & kErrCapacity) return;  // an overflowing sequence draws nothing
   const int ts = __ffs(T) - 1;
-  for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+  const int nv = sc.nviews;
+  for (int c = block; c < nchunks; c += nblocks) {
     // the view of chunk c: the last view whose base is <= c (views without chunks share
     // their successor's base and are never the last such view)
     int lo = 0, hi = nv - 1;
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
-      if ((in_shared ? s_cbase[mid] : views[mid].cch_base) <= c) lo = mid; else hi = mid - 1;
+      if ((cbase ? cbase[mid] : views[mid].cch_base) <= c) lo = mid; else hi = mid - 1;
     }
     const DView& v = views[lo];
     const int W = v.W, npx = v.W * v.H;  // below 2^30 (targets are at most 32768 x 32768)
@@ -214,26 +209,59 @@ __global__ void __launch_bounds__(256) k_clear_empty(const DView* __restrict__ v
     const int i1 = min((c - v.cch_base + 1) * kClearChunk, npx);
     int y = i0 / W, x = i0 - y * W;
     const int qy = 256 / W, qx = 256 - qy * W;  // the step of 256 pixels in rows and columns
-    const uint32_t rgba = v.clear_rgba;
-    const float depth = v.clear_depth;
     const int32_t tb = v.tile_base, tx = v.tiles_x;
-    for (int i = i0; i < i1; i += 256) {
-      if (sc.tile_count[tb + (y >> ts) * tx + (x >> ts)] == 0u) {
-        v.color[i] = rgba;
-        v.depth[i] = depth;
-        if (v.prim) v.prim[i] = 0u;
-      }
+    // all of this thread's tile counts in flight at once, then the stores
+    constexpr int kPer = kClearChunk / 256;
+    uint32_t empty = 0;  // bit k: pixel i0 + 256k is in the chunk and its tile has no record
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+      if (i0 + 256 * k < i1 && sc.tile_count[tb + (y >> ts) * tx + (x >> ts)] == 0u) empty |= 1u << k;
       x += qx;
       y += qy;
       if (x >= W) { x -= W; y++; }
     }
+    if (!empty) continue;
+    const uint32_t rgba = v.clear_rgba;
+    const float depth = v.clear_depth;
+    uint32_t* const prim = v.prim;
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+      if (empty >> k & 1u) {
+        const int i = i0 + 256 * k;
+        v.color[i] = rgba;
+        v.depth[i] = depth;
+        if (prim) prim[i] = 0u;
+      }
+    }
   }
 }
 
-int launch_clear_empty(const DView* views, int tile, int nchunks, Scratch sc, int grid, cudaStream_t s) {
-  if (nchunks <= 0) return 0;
-  const int blocks = grid < nchunks ? (grid > 0 ? grid : 1) : nchunks;
-  k_clear_empty<<<blocks, 256, 0, s>>>(views, tile, nchunks, sc);
+// Scatter and clear in one grid: every kClearEvery-th block clears (when the batch has clear
+// chunks), the others scatter, so the store-bound clear runs beside the atomic-bound scatter
+// instead of after it.
+constexpr int kClearEvery = 2;
+
+__global__ void __launch_bounds__(256) k_scatter(const DView* __restrict__ views, int T, Scratch sc, int nchunks) {
+  __shared__ int32_t s_cbase[kSharedViews];
+  const uint32_t b = blockIdx.x, g = gridDim.x;
+  if (nchunks > 0 && b % kClearEvery == kClearEvery - 1) {  // block-uniform
+    const bool in_shared = sc.nviews <= kSharedViews;
+    if (in_shared)
+      for (int i = threadIdx.x; i < sc.nviews; i += blockDim.x) s_cbase[i] = views[i].cch_base;
+    __syncthreads();
+    clear_empty_tiles(views, T, nchunks, sc, (int)(b / kClearEvery), (int)(g / kClearEvery), in_shared ? s_cbase : nullptr);
+  } else if (nchunks > 0) {
+    scatter_records(views, T, sc, b - b / kClearEvery, g - g / kClearEvery);
+  } else {
+    scatter_records(views, T, sc, b, g);
+  }
+}
+
+// `grid` blocks of 256 threads (at least kClearEvery when the batch clears, so both parts
+// have blocks).
+int launch_scatter(const DView* views, int tile, Scratch sc, int grid, int nchunks, cudaStream_t s) {
+  if (nchunks > 0 && grid < kClearEvery) grid = kClearEvery;
+  k_scatter<<<grid > 0 ? grid : 1, 256, 0, s>>>(views, tile, sc, nchunks);
   return (int)cudaGetLastError();
 }
 
