@@ -119,27 +119,37 @@ __device__ __forceinline__ F3 tex_normal(const DView& v, float u, float t, const
 // `exact` selects the literal divisions; otherwise the sign test on u.x, u.y, u.x+u.y
 // against u.z decides coverage without dividing (equal to the divisions' verdict for
 // coordinates in the range setup checks) and the weights are computed only when covered.
-// The raster and the setup-side cull of pixel-less triangles share this function, so both
+// The raster and the setup-side cull of pixel-less triangles share these functions, so both
 // take the same decision for every pixel.
-__device__ __forceinline__ bool cover_test(float ax, float ay, float e1x, float e1y, float e2x, float e2y, float uz,
-                                           bool exact, float pxf, float pyf, float& b0, float& b1, float& b2) {
-  const float dx = fs(ax, pxf), dy = fs(ay, pyf);
-  const float ux = fs(fm(e1x, dy), fm(dx, e1y));
-  const float uy = fs(fm(dx, e2y), fm(e2x, dy));
-  const float su = fa(ux, uy);
-  if (!exact) {
-    const bool covered = (uz < 0.f) ? (su >= uz && uy <= 0.f && ux <= 0.f) : (su <= uz && uy >= 0.f && ux >= 0.f);
-    if (covered) {
-      b0 = fs(1.f, fd(su, uz));
-      b1 = fd(uy, uz);
-      b2 = fd(ux, uz);
-    }
-    return covered;
-  }
-  b0 = fs(1.f, fd(su, uz));
+//
+// The barycentric weights from the cross products (u.x = ux, u.y = uy, su = ux + uy).
+__device__ __forceinline__ void cover_weights(float ux, float uy, float uz, float& b0, float& b1, float& b2) {
+  b0 = fs(1.f, fd(fa(ux, uy), uz));
   b1 = fd(uy, uz);
   b2 = fd(ux, uz);
+}
+
+// The coverage decision alone, with the cross products the weights come from.
+__device__ __forceinline__ bool cover_terms(float ax, float ay, float e1x, float e1y, float e2x, float e2y, float uz,
+                                            bool exact, float pxf, float pyf, float& ux, float& uy) {
+  const float dx = fs(ax, pxf), dy = fs(ay, pyf);
+  ux = fs(fm(e1x, dy), fm(dx, e1y));
+  uy = fs(fm(dx, e2y), fm(e2x, dy));
+  if (!exact) {
+    const float su = fa(ux, uy);
+    return (uz < 0.f) ? (su >= uz && uy <= 0.f && ux <= 0.f) : (su <= uz && uy >= 0.f && ux >= 0.f);
+  }
+  float b0, b1, b2;
+  cover_weights(ux, uy, uz, b0, b1, b2);
   return !(b0 < 0.f || b1 < 0.f || b2 < 0.f);
+}
+
+__device__ __forceinline__ bool cover_test(float ax, float ay, float e1x, float e1y, float e2x, float e2y, float uz,
+                                           bool exact, float pxf, float pyf, float& b0, float& b1, float& b2) {
+  float ux, uy;
+  const bool covered = cover_terms(ax, ay, e1x, e1y, e2x, e2y, uz, exact, pxf, pyf, ux, uy);
+  if (covered) cover_weights(ux, uy, uz, b0, b1, b2);
+  return covered;
 }
 
 // (float)sqrt(1.0 - (double)s) for s = saturate(...) — the bump height of NormalMapShader

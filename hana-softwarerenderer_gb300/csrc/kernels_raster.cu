@@ -93,6 +93,15 @@ struct BatchRecs {
   uint32_t magic[32];  // ceil(65536 / width): row of a candidate by multiply-shift
 };
 
+// Covered candidates waiting for their weights, depth and visibility update (a ring of 64 per
+// warp): the cross products u.x, u.y of barycentric() and the run | pixel << 8.  The
+// coverage pass fills it at the rate candidates are tested; the weights' three divisions and
+// the depth test then run on full warps of covered candidates.
+struct CandQueue {
+  float ux[64], uy[64];
+  uint32_t jp[64];
+};
+
 // Per-warp tile state in shared memory: per pixel the key (ordered depth | submission) and
 // the index of the record that holds it.  8x8 tiles also keep the winner's payload index,
 // submission number and barycentric weights (28 bytes a pixel), so shading reads no record;
@@ -179,6 +188,7 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
   constexpr int PPL = NPIX / 32;
   __shared__ TileState<NPIX> sst[WARPS];
   __shared__ BatchRecs sbr[WARPS];
+  __shared__ CandQueue scq[WARPS];
   __shared__ float s_u8f[256], s_u8n[256];
   __shared__ int32_t s_tbase[kSharedViews];
   build_byte_tables(s_u8f, s_u8n);
@@ -190,6 +200,7 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   TileState<NPIX>& st = sst[warp];
   BatchRecs& br = sbr[warp];
+  CandQueue& cq = scq[warp];
   if (sc.ctl->error & kErrCapacity) return;
   const uint32_t nrec = min(sc.ctl->rec_count, sc.rec_cap);
 
@@ -294,6 +305,41 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
           br.magic[k] = kDivMagic[box >> 16];
         }
         __syncwarp();
+        // Visibility of `cnt` queued candidates from the ring head, one per lane: weights
+        // (the divisions of barycentric()), depth, and a 64-bit atomicMin of the key.
+        uint32_t qh = 0, qn = 0;  // ring head and queued count (warp-uniform)
+        auto resolve = [&](uint32_t cnt) {
+          __syncwarp();
+          const bool act = (uint32_t)lane < cnt;
+          unsigned long long key = 0ull, old = 0ull;
+          int p = 0, j = 0;
+          float b0 = 0.f, b1 = 0.f, b2 = 0.f;
+          if (act) {
+            const uint32_t e = (qh + (uint32_t)lane) & 63u;
+            const uint32_t jp = cq.jp[e];
+            j = (int)(jp & 31u);
+            p = (int)(jp >> 8);
+            cover_weights(cq.ux[e], cq.uy[e], br.uz[j], b0, b1, b2);
+            // interpolate_depth (graphics.cpp:186-194)
+            const float z = fa(fa(fa(0.f, fm(br.d2[j], b2)), fm(br.d1[j], b1)), fm(br.d0[j], b0));
+            key = ((unsigned long long)ord_bits(z) << 32) | (unsigned long long)(0xfffffffeu - br.seq[j]);
+            old = atomicMin(&st.key[p], key);
+          }
+          __syncwarp();
+          if (act && old > key && st.key[p] == key) {
+            st.rec[p] = br.idx[j];
+            if constexpr (TileState<NPIX>::kKeep) {
+              st.pay[p] = br.pay[j];
+              st.seq[p] = br.seq[j];
+              st.b0[p] = b0;
+              st.b1[p] = b1;
+              st.b2[p] = b2;
+            }
+          }
+          qh = (qh + cnt) & 63u;
+          qn -= cnt;
+          __syncwarp();
+        };
         for (uint32_t base = 0; base < W; base += 32) {
           // runs starting before this window, and a bit per run starting inside it
           const uint32_t before = (uint32_t)__popc(__ballot_sync(kFull, c > 0u && start < base));
@@ -301,9 +347,8 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
               kFull, (c > 0u && start >= base && start - base < 32u) ? 1u << (start - base) : 0u);
           const uint32_t i = base + (uint32_t)lane;
           bool covered = false;
-          unsigned long long key = 0ull, old = 0ull;
+          float ux = 0.f, uy = 0.f;
           int p = 0, j = 0;
-          float b0 = 0.f, b1 = 0.f, b2 = 0.f;
           if (i < W) {
             // owner: the last run starting at or before candidate i
             j = (int)(before + (uint32_t)__popc(here & ((2u << lane) - 1u))) - 1;
@@ -314,29 +359,21 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
             const int lx = (int)(bx & 255u) + (int)(q - qy * lw);
             const int ly = (int)((bx >> 8) & 255u) + (int)qy;
             p = ly * T + lx;
-            covered = cover_test(br.ax[j], br.ay[j], br.e1x[j], br.e1y[j], br.e2x[j], br.e2y[j], br.uz[j],
-                                 (bx >> 31) != 0u, (float)(ox + lx), (float)(oy + ly), b0, b1, b2);
-            if (covered) {
-              frags++;
-              // interpolate_depth (graphics.cpp:186-194)
-              const float z = fa(fa(fa(0.f, fm(br.d2[j], b2)), fm(br.d1[j], b1)), fm(br.d0[j], b0));
-              key = ((unsigned long long)ord_bits(z) << 32) | (unsigned long long)(0xfffffffeu - br.seq[j]);
-              old = atomicMin(&st.key[p], key);
-            }
+            covered = cover_terms(br.ax[j], br.ay[j], br.e1x[j], br.e1y[j], br.e2x[j], br.e2y[j], br.uz[j],
+                                  (bx >> 31) != 0u, (float)(ox + lx), (float)(oy + ly), ux, uy);
           }
-          __syncwarp();
-          if (covered && old > key && st.key[p] == key) {
-            st.rec[p] = br.idx[j];
-            if constexpr (TileState<NPIX>::kKeep) {
-              st.pay[p] = br.pay[j];
-              st.seq[p] = br.seq[j];
-              st.b0[p] = b0;
-              st.b1[p] = b1;
-              st.b2[p] = b2;
-            }
+          const unsigned cm = __ballot_sync(kFull, covered);
+          if (covered) {  // queue behind the pending ones (at most 31 are pending here)
+            frags++;
+            const uint32_t e = (qh + qn + (uint32_t)__popc(cm & ((1u << lane) - 1u))) & 63u;
+            cq.ux[e] = ux;
+            cq.uy[e] = uy;
+            cq.jp[e] = (uint32_t)j | ((uint32_t)p << 8);
           }
-          __syncwarp();
+          qn += (uint32_t)__popc(cm);
+          if (qn >= 32u) resolve(32u);
         }
+        if (qn) resolve(qn);  // before the next batch replaces the runs the queue points to
       }
       __syncwarp();
       uint32_t shaded = 0;
