@@ -165,20 +165,23 @@ def kernel_bytes(t: dict) -> dict:
     setup  : 16 B index read + 16 B clip read per face corner set (each vertex once) + a
              64 B record written per triangle that reaches the raster.
     scan   : 4 B read + 4 B written per tile.
-    scatter: 16 B of each record read + 4 B written per (triangle, tile) pair.
-    raster : 12 B written per pixel (colour, depth, prim id; the clear is fused), 4 B read
+    scatter: 16 B of each record read + 4 B written per (triangle, tile) pair, and the fused
+             clear of the tiles without triangles: 12 B written per pixel (colour, depth,
+             prim id) outside the raster's tiles.
+    raster : 12 B written per pixel of the tiles it visits (colour, depth, prim id), 4 B read
              per (triangle, tile) pair + the 64 B record, and per shaded pixel the texels it
              samples (diffuse, normal map, shadow map: 4 B each) — vertex attributes of the
              visible triangles are counted once per record (3 corners x 56 B).
     """
     px, rec, pairs = t["pixels"], t["records"], t["bin_pairs"]
+    rpx = t.get("raster_pixels", px)
     tiles = px / 64.0  # tiles of the scan, counted as 8x8 (the 16x16 grid has fewer)
     return {
         "vertex": t["vertices"] * 28 + t["vertices"] * 8 + t["normals"] * 28,
         "setup": t["faces"] * 16 + t["vertices"] * 16 + rec * 64,
         "scan": tiles * 8,
-        "scatter": rec * 16 + pairs * 4,
-        "raster": px * 12 + pairs * 4 + rec * (64 + 3 * 56) + t["shaded_pixels"] * 12,
+        "scatter": rec * 16 + pairs * 4 + (px - rpx) * 12,
+        "raster": rpx * 12 + pairs * 4 + rec * (64 + 3 * 56) + t["shaded_pixels"] * 12,
     }
 
 
@@ -269,7 +272,8 @@ def run_ours(args, world, rank, local):
         launches += int(t["launches"])
         h2d.append(int(t["h2d_bytes"]))
         d2h.append(sum(r.width * r.height * 4 for r in chunk) + int(t["d2h_bytes"]))
-        for k in ("faces", "vertices", "normals", "records", "bin_pairs", "pixels", "shaded_pixels", "clipped_faces"):
+        for k in ("faces", "vertices", "normals", "records", "bin_pairs", "pixels", "shaded_pixels", "clipped_faces",
+                  "raster_pixels"):
             counts_sum[k] = counts_sum.get(k, 0) + int(t[k])
     torch.cuda.synchronize()
     clocks = sampler.stop()
@@ -390,7 +394,7 @@ def run_frame(args) -> dict:
         plain.append((time.perf_counter() - s0) * 1000.0)
     hsr.set_profiling(False)
     counts = {k: int(t[k]) for k in ("faces", "vertices", "normals", "records", "bin_pairs", "pixels",
-                                     "shaded_pixels", "clipped_faces")}
+                                     "shaded_pixels", "clipped_faces", "raster_pixels")}
     res = {"workload": FRAME_WORKLOAD, "frames_per_s": round(1000.0 / statistics.mean(ms), 2),
            "ms_p50": round(float(np.percentile(ms, 50)), 4), "ms_p99": round(float(np.percentile(ms, 99)), 4),
            "plain_two_draw_calls_frames_per_s": round(1000.0 / statistics.mean(plain), 2),
@@ -430,7 +434,7 @@ def run_soup(args) -> dict:
             kms[k].append(v)
     hsr.set_profiling(False)
     counts = {k: int(t[k]) for k in ("faces", "vertices", "normals", "records", "bin_pairs", "pixels",
-                                     "shaded_pixels", "fragments", "clipped_faces")}
+                                     "shaded_pixels", "fragments", "clipped_faces", "raster_pixels")}
     s = statistics.mean(ms) / 1000.0
     res = {"workload": SOUP_WORKLOAD, "frames_per_s": round(1.0 / s, 2), "ms": round(s * 1000.0, 4),
            "mtris_per_s": round(counts["faces"] / s / 1e6, 1),

@@ -391,6 +391,7 @@ void Runtime::record_result(const Plan& p, const Ctl& c) {
   timing.bin_pairs = c.bin_total;
   timing.shaded_pixels = c.shaded_px;
   timing.fragments = c.frag_px;
+  timing.raster_pixels = std::min<uint64_t>((uint64_t)c.ne_tiles * (uint64_t)p.tile * (uint64_t)p.tile, p.total_pixels);
   timing.pixels = p.total_pixels;
   timing.faces = p.total_faces;
   timing.vertices = p.total_pos;

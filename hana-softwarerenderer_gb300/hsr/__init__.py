@@ -51,7 +51,8 @@ class Timing(ctypes.Structure):
                 ("views", ctypes.c_uint32), ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
                 ("pixels", ctypes.c_uint64), ("shaded_pixels", ctypes.c_uint64), ("records", ctypes.c_uint64),
                 ("bin_pairs", ctypes.c_uint64), ("faces", ctypes.c_uint64), ("vertices", ctypes.c_uint64),
-                ("normals", ctypes.c_uint64), ("clipped_faces", ctypes.c_uint64), ("fragments", ctypes.c_uint64)]
+                ("normals", ctypes.c_uint64), ("clipped_faces", ctypes.c_uint64), ("fragments", ctypes.c_uint64),
+                ("raster_pixels", ctypes.c_uint64)]
 
 
 KERNELS = ("vertex", "setup", "scan", "scatter", "raster")

@@ -351,6 +351,8 @@ typedef struct hsr_timing {
   uint64_t normals;        /* normals transformed                                      */
   uint64_t clipped_faces;  /* faces that went through the homogeneous clipper          */
   uint64_t fragments;      /* covered (pixel, triangle) pairs tested against the depth  */
+  uint64_t raster_pixels;  /* pixels of the tiles the raster visited (tiles with triangles;
+                              the fused clear of the others runs beside the binning)    */
 } hsr_timing;
 HSR_API int hsr_set_profiling(int on);
 HSR_API int hsr_last_timing(hsr_timing* out);

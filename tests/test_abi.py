@@ -65,7 +65,7 @@ def test_struct_layouts_match_header(tmp_path):
         "hsr_request": (hsr.Request, ["uniforms", "clear_rgba", "shadow_clear_depth", "out_rgba", "out_prim"]),
         "hsr_request_status": (hsr.RequestStatus, ["submit_ms", "done_ms"]),
         "hsr_server_config": (hsr.ServerConfig, ["max_batch", "slots"]),
-        "hsr_timing": (hsr.Timing, ["launches", "h2d_bytes", "clipped_faces", "fragments"]),
+        "hsr_timing": (hsr.Timing, ["launches", "h2d_bytes", "clipped_faces", "fragments", "raster_pixels"]),
         "hsr_stats": (hsr.Stats, ["kernel_launches"]),
         "hsr_tuning": (hsr.Tuning, ["bin_factor"]),
         "hsr_transform": (hsr.Transform, ["rotation", "scale"]),
