@@ -60,6 +60,7 @@ FOVY = to_radians(60)          # camera.cpp:13
 NEAR = F32(0.1)                # camera.cpp:11
 FAR = F32(10000)               # camera.cpp:12
 UP = (F32(0), F32(1), F32(0))  # camera.cpp:14
+ORIGIN = (F32(0), F32(0), F32(0))  # Camera::get_target_position (camera.cpp:94-97)
 
 AMBIENT = (F32(54) / F32(255), F32(58) / F32(255), F32(66) / F32(255), F32(255))        # scene.h:8
 LIGHT_COLOR = (F32(255) / F32(255), F32(244) / F32(255), F32(214) / F32(255), F32(255))  # scene.h:9
@@ -210,10 +211,12 @@ def shader_data(eye, width: int, height: int, *, target=(0, 0, 0), light=LIGHT_P
             model_I = _IDENTITY_INV
         else:
             model_I = model.invert()
-        lvp = orthographic(aspect, 1, 0, 5) @ lookat(light, target, UP)
+        # the light looks at Camera::get_target_position(), which returns the origin whatever
+        # the camera's target (camera.cpp:94-97)
+        lvp = orthographic(aspect, 1, 0, 5) @ lookat(light, ORIGIN, UP)
         cvp = proj @ view
     sd["view_pos"] = eye
-    sd["light_dir"] = normalize3(sub3(light, target))
+    sd["light_dir"] = normalize3(sub3(light, ORIGIN))
     sd["light_color"] = LIGHT_COLOR
     sd["ambient"] = AMBIENT
     sd["model_matrix"] = model.flat()

@@ -12,6 +12,7 @@ import golden_io
 import oracle
 from hsr import frame as hframe
 from hsr import scenes
+from hsr import uniforms as U
 
 pytestmark = pytest.mark.gpu
 
@@ -236,6 +237,54 @@ def test_empty_mesh_only_clears(gpu):
         tgt.release()
     assert (got["color"] == np.array([1, 2, 3, 4], np.uint8)).all()
     assert (got["depth"] == np.float32(0.5)).all() and (got["prim"] == 0).all()
+
+
+def _light_far_frame():
+    """A shadowed frame whose shadow pass has no triangle: the light sits 40 units out, beyond
+    the far plane of its orthographic volume (depth 0..5), while the camera sees the mesh."""
+    f = scenes.sphere_frame(3, 96, 72, shader=scenes.BLINN, tex_size=32, seed=3, shadow=64)
+    f.sd = U.shader_data((0.0, 0.0, 3.0), 96, 72, light=(0.0, 0.0, 40.0), enable_shadow=True)
+    f.name = "light_far"
+    return f
+
+
+def _looking_away_frame():
+    """A shadowed frame whose main pass has no triangle (every face is behind the camera)
+    while its shadow pass has many: all main pixels come from the clear of empty tiles."""
+    f = scenes.sphere_frame(3, 80, 64, shader=scenes.NORMALMAP, tex_size=32, seed=4, shadow=64, nm_size=16)
+    f.sd = U.shader_data((0.0, 0.0, 3.0), 80, 64, target=(0.0, 0.0, 6.0), enable_shadow=True)
+    f.name = "looking_away"
+    return f
+
+
+@pytest.mark.parametrize("make", [_light_far_frame, _looking_away_frame])
+def test_views_without_triangles_vs_oracle(gpu, make):
+    """A view with no triangle has no tile in the raster's list: its pixels come from the
+    clear that runs beside the binning, and a view waiting on it (the main pass on its shadow
+    map) waits for nothing."""
+    fr = make()
+    exp = oracle_expect(fr)
+    assert_parity(gpu_render(gpu, fr, batched=True), exp, fr.name + " batched")
+    assert_parity(gpu_render(gpu, fr, batched=False), exp, fr.name + " per pass")
+
+
+def test_batch_mixing_empty_and_full_views_vs_oracle(gpu):
+    """One launch sequence over frames whose shadow or main pass is empty and a normal frame,
+    each with its own targets: the non-empty tile list spans views with and without
+    triangles, and each main pass waits on its own shadow map only."""
+    import hsr
+
+    frames = [_light_far_frame(), scenes.sphere_frame(3, 72, 56, shader=scenes.TOON, tex_size=16, seed=6, shadow=32),
+              _looking_away_frame()]
+    gfs = [hframe.GpuFrame(f) for f in frames]
+    try:
+        hsr.draw_batch([d for g in gfs for d in g.descs])
+        got = [g.download() for g in gfs]
+    finally:
+        for g in gfs:
+            g.release()
+    for f, g in zip(frames, got):
+        assert_parity(g, oracle_expect(f), f.name + " in a mixed batch")
 
 
 def test_autotune_picks_a_valid_config_and_stays_exact(gpu):

@@ -44,6 +44,15 @@ def test_matches_python_builder(eye, w, h):
         assert np.array_equal(np.asarray(a[k]).reshape(-1).view(np.uint32), np.asarray(b[k]).reshape(-1).view(np.uint32)), k
 
 
+def test_python_builder_with_a_camera_target_lights_from_the_origin():
+    """The light looks at Camera::get_target_position(), the origin whatever the camera's
+    target (camera.cpp:94-97), in both builders."""
+    a = hsr.shader_data_build((0.5, 0.4, 3.0), 320, 200, camera_target=(0.3, -0.2, 6.0), enable_shadow=True)
+    b = U.shader_data((0.5, 0.4, 3.0), 320, 200, target=(0.3, -0.2, 6.0), enable_shadow=True)
+    for k in FIELDS:
+        assert np.array_equal(np.asarray(a[k]).reshape(-1).view(np.uint32), np.asarray(b[k]).reshape(-1).view(np.uint32)), k
+
+
 def test_invert_of_identity_has_the_reference_signed_zeros():
     inv = hsr.matrix_invert(np.eye(4, dtype=np.float32))
     py = U.Mat4.identity().invert().flat()
