@@ -288,16 +288,26 @@ def run_ours(args, world, rank, local):
     # ---- e2e: the same requests through hsr_server (all submitted at once) ----------------
     timed_reqs = [r for c in chunks[args.warmup:] for r in c]
     sat = scenes.retime(timed_reqs, 1e9)
-    hserve.serve_batched(rp, scenes.retime([r for c in chunks[:args.warmup] for r in c], 1e9), max_batch=BATCH)
-    dist_barrier(world)
-    e2e_run = hserve.serve_batched(rp, sat, max_batch=BATCH, slots=2)
+    # one long-running server: the warm-up requests pass through it first (its scratch and the
+    # memory pool reach their working size there), then the timed ones
+    srv = hsr.Server(40 << 30, BATCH, 2)
+    ring = hserve.PinnedRing(1 << 30)
+    try:
+        hserve.serve_batched(rp, scenes.retime([r for c in chunks[:args.warmup] for r in c], 1e9), server=srv,
+                             ring=ring)
+        dist_barrier(world)
+        e2e_run = hserve.serve_batched(rp, sat, server=srv, ring=ring)
+    finally:
+        srv.close()
+        ring.release()
     e2e_s = dist_max(e2e_run["wall_s"], world)
     e2e = {"value": round(world * frames / e2e_s, 2), "unit": "frames/s",
            "h2d_bytes_per_step": int(statistics.mean(h2d)), "d2h_bytes_per_step": int(statistics.mean(d2h)),
            "p50_ms": round(float(np.percentile(e2e_run["latency_ms"], 50)), 3),
            "p99_ms": round(float(np.percentile(e2e_run["latency_ms"], 99)), 3),
            "batches": e2e_run["batches"], "ok": e2e_run["ok"],
-           "note": "hsr_server, max_batch 64, 2 slots; all requests submitted at t=0; wall clock"}
+           "note": "hsr_server, max_batch 64, 2 slots, warmed by the warm-up steps' requests; all timed "
+                   "requests submitted at t=0; wall clock"}
 
     out = {
         "metric": METRIC, "value": round(value, 2), "unit": "frames/s", "n_gpus": world,

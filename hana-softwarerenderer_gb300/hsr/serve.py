@@ -151,11 +151,19 @@ def _wait_until(t0: float, ms: float) -> None:
 
 
 def serve_batched(rp: ResidentPool, reqs: list, pool_bytes: int = 40 << 30, max_batch: int = 64, slots: int = 2,
-                  ring_bytes: int = 1 << 30, keep_outputs: bool = False) -> dict:
+                  ring_bytes: int = 1 << 30, keep_outputs: bool = False, server: Server | None = None,
+                  ring: "PinnedRing | None" = None) -> dict:
     """Submit `reqs` (scenes.Request) at their arrival times to an hsr_server; return
-    per-request latency (done - scheduled arrival) and the run's wall time."""
-    srv = Server(pool_bytes, max_batch, slots)
-    ring = PinnedRing(ring_bytes)
+    per-request latency (done - scheduled arrival) and the run's wall time.  A `server` and
+    `ring` passed in are used as they are and stay open (a long-running server across calls);
+    otherwise both are made for this call and closed at its end."""
+    own = server is None
+    srv = server if server is not None else Server(pool_bytes, max_batch, slots)
+    if ring is None:
+        ring = PinnedRing(ring_bytes)
+        own_ring = True
+    else:
+        own_ring = False
     outstanding: collections.deque = collections.deque()
     status: dict[int, dict] = {}
     outputs: dict[int, np.ndarray] = {}
@@ -202,8 +210,10 @@ def serve_batched(rp: ResidentPool, reqs: list, pool_bytes: int = 40 << 30, max_
             reclaim_one()
         wall = time.perf_counter() - t0
     finally:
-        srv.close()
-        ring.release()
+        if own:
+            srv.close()
+        if own_ring:
+            ring.release()
     lat = np.array([status[i]["done_ms"] - (srv_t0 + reqs[i].arrival_ms) for i in range(len(reqs))])
     ok = all(status[i]["status"] == 0 for i in range(len(reqs)))
     batches = {status[i]["batch"]: status[i]["batch_requests"] for i in range(len(reqs))}
