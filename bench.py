@@ -160,8 +160,9 @@ def dist_barrier(world: int):
 def kernel_bytes(t: dict) -> dict:
     """Algorithmic bytes per launch of each kernel of one launch sequence.
 
-    vertex : 12 B read + 16 B clip written per position, +16 B world position where the
-             shader reads it; 12 B read + 16 B written per normal.
+    vertex : 12 B read + 16 B screen vertex written per position (world positions and
+             normals are transformed per corner of the surviving triangles, in the setup
+             segment).
     setup  : 16 B index read + 16 B clip read per face corner set (each vertex once) + a
              64 B record written per triangle that reaches the raster.
     scan   : 4 B read + 4 B written per tile.
@@ -177,7 +178,7 @@ def kernel_bytes(t: dict) -> dict:
     rpx = t.get("raster_pixels", px)
     tiles = px / 64.0  # tiles of the scan, counted as 8x8 (the 16x16 grid has fewer)
     return {
-        "vertex": t["vertices"] * 28 + t["vertices"] * 8 + t["normals"] * 28,
+        "vertex": t["vertices"] * 28 + t["normals"] * 28,
         "setup": t["faces"] * 16 + t["vertices"] * 16 + rec * 64,
         "scan": tiles * 8,
         "scatter": rec * 16 + pairs * 4 + (px - rpx) * 12,

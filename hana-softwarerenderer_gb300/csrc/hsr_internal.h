@@ -1,7 +1,8 @@
 // hsr_internal.h — data layout shared by the host runtime and the sm_103a kernels.
 //
 // Pipeline of one launch sequence (a batch of views = draws):
-//   k_vertex  : SoA attribute streams -> screen vertex / world position / world normal per view
+//   k_vertex  : SoA positions -> screen vertex per view (world attributes are transformed per
+//               corner where a triangle survives: k_emit, and the clipper)
 //   k_setup   : per face: fast accept or homogeneous clip (graphics.cpp:132-161), then per
 //               fan triangle divide / cull / viewport / bbox (graphics.cpp:314-347) -> one
 //               64-byte RasterRec, plus per-tile counts (warp-aggregated atomics)
@@ -96,10 +97,12 @@ struct __align__(128) DView {
   const int4* fv; const int4* fvt; const int4* fvn;    // per-face corner indices (+pad)
   int32_t npos, nnrm, nuv, nfaces;
   int32_t unified;  // every face corner has equal v, vt and vn indices (fvt, fvn unused)
+  // the mesh's positions and normals as (x, y, z, 0), gathered per corner for the world
+  // attributes, and which of those the view's shader reads (kWorld*)
+  const float4* p4; const float4* n4;
+  uint32_t world;
   // vertex outputs (scratch)
   float4* sv;     // [npos] screen vertex: (x/w, y/w, z/w, 1/w) or plane mask (k_vertex)
-  float4* wpos;   // [npos] or null
-  float4* wnrm;   // [nnrm] (xyz, intensity) or null
   // shading
   float mvp[16];        // camera_vp*model (light_vp*model for SHADOW), host-computed
   hsr_shader_data u;
@@ -108,14 +111,15 @@ struct __align__(128) DView {
   // shadow map (colour plane of another target), null when ShaderData::shadow_map is null
   const uint32_t* sm_color; int32_t smW, smH;
   // this view's work chunks in the batch's chunk spaces (a kernel finds the view of chunk c
-  // as the last view whose base is <= c): vertex chunks of kVertexChunk items (its position
-  // chunks, then its normal chunks), setup chunks of kSetupChunk faces, clear chunks of
-  // kClearChunk pixels (none for a view drawn without the fused clear)
+  // as the last view whose base is <= c): vertex chunks of kVertexChunk positions, setup
+  // chunks of kSetupChunk faces, clear chunks of kClearChunk pixels (none for a view drawn
+  // without the fused clear)
   int32_t vch_base, vch_npos, vch_count;
   int32_t sch_base;
   int32_t cch_base;
 };
-constexpr int kVertexChunk = 2048;  // positions or normals per vertex-stage chunk
+constexpr int kVertexChunk = 2048;  // positions per vertex-stage chunk
+constexpr uint32_t kWorldPos = 1u, kWorldNormal = 2u;  // DView::world
 constexpr int kSetupChunk = 256;    // faces per setup chunk (one per thread of a block)
 constexpr int kClearChunk = 4096;   // pixels per clear chunk (16 per thread of a block)
 constexpr int64_t kMaxBatchTiles = (int64_t)1 << 26;  // tiles of one launch sequence (scan word)

@@ -78,6 +78,8 @@ static int noalloc_draw(Runtime* rt, const hsr_draw_desc& d) {
   std::memset(&v, 0, sizeof(v));
   v.px = m->px; v.py = m->py; v.pz = m->pz;
   v.nx = m->nx; v.ny = m->ny; v.nz = m->nz;
+  v.p4 = m->p4; v.n4 = m->n4;
+  v.world = (needs_wpos_h(d.shader) ? kWorldPos : 0u) | (needs_wnrm_h(d.shader) ? kWorldNormal : 0u);
   v.uv = m->uv;
   v.fv = m->fv; v.fvt = m->fvt; v.fvn = m->fvn;
   v.npos = m->npos; v.nnrm = m->nnrm; v.nuv = m->nuv; v.nfaces = m->nfaces;
@@ -110,10 +112,9 @@ static int noalloc_draw(Runtime* rt, const hsr_draw_desc& d) {
   v.has_dependents = 0;
 
   // ---- work chunks and the fixed layout of the static array ------------------------------
-  const bool wnrm = needs_wnrm_h(d.shader);
   v.vch_base = 0;
   v.vch_npos = (m->npos + kVertexChunk - 1) / kVertexChunk;
-  v.vch_count = v.vch_npos + (wnrm ? (m->nnrm + kVertexChunk - 1) / kVertexChunk : 0);
+  v.vch_count = v.vch_npos;
   v.sch_base = 0;
   v.cch_base = 0;
   const int nvch = v.vch_count;
@@ -127,8 +128,6 @@ static int noalloc_draw(Runtime* rt, const hsr_draw_desc& d) {
   const size_t o_view = off; off = nal(off + sizeof(DView));
   const size_t host_bytes = off;
   const size_t o_clip = off; off = nal(off + sizeof(float4) * (size_t)std::max(m->npos, 1));
-  const size_t o_wpos = off; if (needs_wpos_h(d.shader)) off = nal(off + sizeof(float4) * (size_t)std::max(m->npos, 1));
-  const size_t o_wnrm = off; if (wnrm) off = nal(off + sizeof(float4) * (size_t)std::max(m->nnrm, 1));
   const size_t o_zero = off;
   const size_t o_ctl = off; off = nal(off + sizeof(Ctl));
   const size_t o_done = off; off = nal(off + sizeof(uint32_t));
@@ -148,8 +147,6 @@ static int noalloc_draw(Runtime* rt, const hsr_draw_desc& d) {
     return fail(HSR_ERR_INVALID_ARG, "draw_noalloc: the draw needs more scratch than the 128 MiB the allocation-free path holds");
 
   v.sv = (float4*)(dev + o_clip);
-  v.wpos = needs_wpos_h(d.shader) ? (float4*)(dev + o_wpos) : nullptr;
-  v.wnrm = wnrm ? (float4*)(dev + o_wnrm) : nullptr;
 
   unsigned char* h = g_noalloc_host;
   std::memcpy(h + o_view, &v, sizeof(DView));

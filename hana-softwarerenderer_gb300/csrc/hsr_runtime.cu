@@ -69,8 +69,8 @@ static int dalloc(void** p, size_t bytes, const char* what) {
 }
 
 MeshObj::~MeshObj() {
-  for (void* p : {(void*)px, (void*)py, (void*)pz, (void*)nx, (void*)ny, (void*)nz, (void*)uv, (void*)fv,
-                  (void*)fvt, (void*)fvn})
+  for (void* p : {(void*)px, (void*)py, (void*)pz, (void*)nx, (void*)ny, (void*)nz, (void*)p4, (void*)n4, (void*)uv,
+                  (void*)fv, (void*)fvt, (void*)fvn})
     if (p) cudaFree(p);
 }
 TexObj::~TexObj() {
@@ -196,6 +196,8 @@ int Runtime::plan_build(const hsr_draw_desc* descs, int n, Plan& p) {
     std::memset(&v, 0, sizeof(v));
     v.px = m->px; v.py = m->py; v.pz = m->pz;
     v.nx = m->nx; v.ny = m->ny; v.nz = m->nz;
+    v.p4 = m->p4; v.n4 = m->n4;
+    v.world = (shader_needs_wpos(d.shader) ? kWorldPos : 0u) | (shader_needs_wnrm(d.shader) ? kWorldNormal : 0u);
     v.uv = m->uv;
     v.fv = m->fv; v.fvt = m->fvt; v.fvn = m->fvn;
     v.npos = m->npos; v.nnrm = m->nnrm; v.nuv = m->nuv; v.nfaces = m->nfaces;
@@ -232,16 +234,9 @@ int Runtime::plan_build(const hsr_draw_desc* descs, int n, Plan& p) {
     p.total_pixels += (size_t)tg->w * (size_t)tg->h;
     Plan::Off& o = p.offs[k];
     o.clip = bytes; bytes = align_up(bytes + sizeof(float4) * (size_t)std::max(m->npos, 1), 256);
-    o.wpos = bytes;
-    if (shader_needs_wpos(d.shader)) bytes = align_up(bytes + sizeof(float4) * (size_t)std::max(m->npos, 1), 256);
-    o.wnrm = bytes;
-    if (shader_needs_wnrm(d.shader)) {
-      bytes = align_up(bytes + sizeof(float4) * (size_t)std::max(m->nnrm, 1), 256);
-      p.total_nrm += (size_t)m->nnrm;
-    }
     v.vch_base = p.nvch;
     v.vch_npos = (m->npos + kVertexChunk - 1) / kVertexChunk;
-    v.vch_count = v.vch_npos + (shader_needs_wnrm(d.shader) ? (m->nnrm + kVertexChunk - 1) / kVertexChunk : 0);
+    v.vch_count = v.vch_npos;
     v.sch_base = p.nsch;
     v.cch_base = p.ncch;
     p.nvch += v.vch_count;
@@ -300,8 +295,6 @@ void Plan::bind(char* dev_base, char* host_base) {
   for (int k = 0; k < n; k++) {
     DView& v = views[k];
     v.sv = (float4*)(dev + o_vout + offs[k].clip);
-    v.wpos = shader_needs_wpos(v.shader) ? (float4*)(dev + o_vout + offs[k].wpos) : nullptr;
-    v.wnrm = shader_needs_wnrm(v.shader) ? (float4*)(dev + o_vout + offs[k].wnrm) : nullptr;
   }
   std::memcpy(host + o_views, views.data(), sizeof(DView) * n);
   sc.ctl = (Ctl*)(dev + o_ctl);
@@ -537,6 +530,18 @@ int hsr_shutdown(void) {
   return HSR_OK;
 }
 
+// (x, y, z, 0) per item of an xyz array into a device array of max(n, 1) float4s.
+static int write_xyz0(const float* src, int32_t n, float4* dst) {
+  std::vector<float4> tmp((size_t)std::max(n, 1), make_float4(0.f, 0.f, 0.f, 0.f));
+  for (int32_t i = 0; i < n; i++) tmp[i] = make_float4(src[(size_t)i * 3], src[(size_t)i * 3 + 1], src[(size_t)i * 3 + 2], 0.f);
+  cudaError_t e = cudaMemcpy(dst, tmp.data(), sizeof(float4) * tmp.size(), cudaMemcpyHostToDevice);
+  return e == cudaSuccess ? HSR_OK : cuda_fail(e, "mesh upload");
+}
+static int upload_xyz0(const float* src, int32_t n, float4** dst) {
+  int rc = dalloc((void**)dst, sizeof(float4) * (size_t)std::max(n, 1), "mesh");
+  return rc == HSR_OK ? write_xyz0(src, n, *dst) : rc;
+}
+
 int hsr_mesh_upload(const float* pos, int32_t npos, const float* nrm, int32_t nnrm, const float* uv, int32_t nuv,
                     const int32_t* faces, int32_t nfaces, hsr_mesh* out) {
   RT_OR_FAIL();
@@ -564,6 +569,8 @@ int hsr_mesh_upload(const float* pos, int32_t npos, const float* nrm, int32_t nn
   };
   for (int c = 0; c < 3 && rc == HSR_OK; c++) rc = up_soa(pos, npos, c, P, c == 0 ? &m->px : (c == 1 ? &m->py : &m->pz));
   for (int c = 0; c < 3 && rc == HSR_OK; c++) rc = up_soa(nrm, nnrm, c, N, c == 0 ? &m->nx : (c == 1 ? &m->ny : &m->nz));
+  if (rc == HSR_OK) rc = upload_xyz0(pos, npos, &m->p4);
+  if (rc == HSR_OK) rc = upload_xyz0(nrm, nnrm, &m->n4);
   if (rc == HSR_OK) rc = dalloc((void**)&m->uv, sizeof(float2) * (size_t)std::max(nuv, 1), "mesh uv");
   if (rc == HSR_OK && nuv) {
     cudaError_t e = cudaMemcpy(m->uv, uv, sizeof(float2) * (size_t)nuv, cudaMemcpyHostToDevice);
@@ -612,7 +619,7 @@ int hsr_mesh_update_normals(hsr_mesh mh, const float* nrm, int32_t nnrm) {
     cudaError_t e = cudaMemcpy(dst[c], tmp.data(), sizeof(float) * N, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_fail(e, "normal upload");
   }
-  return HSR_OK;
+  return write_xyz0(nrm, nnrm, m->n4);
 }
 
 int hsr_mesh_release(hsr_mesh mh) {

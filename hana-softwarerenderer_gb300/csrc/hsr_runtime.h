@@ -15,6 +15,7 @@ namespace hsr {
 struct MeshObj {  // Model (model.h:8-33) resident on the device
   float *px = nullptr, *py = nullptr, *pz = nullptr;
   float *nx = nullptr, *ny = nullptr, *nz = nullptr;
+  float4 *p4 = nullptr, *n4 = nullptr;  // positions and normals as (x, y, z, 0)
   float2* uv = nullptr;
   int4 *fv = nullptr, *fvt = nullptr, *fvn = nullptr;
   int32_t npos = 0, nnrm = 0, nuv = 0, nfaces = 0;
@@ -53,7 +54,7 @@ struct Pinned {  // grow-only pinned host staging
 
 // One launch sequence: view descriptors, work chunks, scratch layout and capacities.
 struct Plan {
-  struct Off { size_t clip, wpos, wnrm; };
+  struct Off { size_t clip; };
   int n = 0, tile = 8, nscan = 0;
   std::vector<int> order;         // plan position -> index in the caller's array
   std::vector<DView> views;

@@ -3,12 +3,15 @@
 // k_vertex replaces the per-corner IShader::vertex calls of graphics.cpp:380-387.  The
 // vertex shader is a pure function of its a2v inputs, and each output stream depends on
 // one attribute stream only (clip and world position on `v`, world normal and light
-// intensity on `vn`, uv passes through), so each attribute is transformed once and the
-// setup kernel gathers per corner: the same bits as three vertex() calls per face.  The
+// intensity on `vn`, uv passes through), so every corner gets the same bits whether an
+// output is computed once per vertex or once per corner.  The clip position and the
 // per-corner work of rasterize_triangle that depends on one vertex alone — the visibility
 // test of clip_triangle's fast accept (graphics.cpp:132-134, 140-142) and, for a visible
-// vertex, the perspective divide and 1/w (:320-337) — is done here once per vertex too
-// (the screen vertex, see screen_vertex), so setup divides nothing on the fast path.
+// vertex, the perspective divide and 1/w (:320-337) — is done here once per vertex (the
+// screen vertex, see screen_vertex), so setup divides nothing on the fast path.  World
+// position and normal are needed only for the corners of the one triangle in five that
+// survives setup: k_emit (and the clipper) transform them per corner (world_pos_of,
+// world_normal_of) instead of this pass writing and re-reading them for every vertex.
 //
 // k_setup follows graphics.cpp:136-161 (clip) and :314-347 (cull, viewport, bounding box)
 // for every fan triangle and emits one RasterRec.  Faces that fail the fast accept are
@@ -82,6 +85,25 @@ __device__ __forceinline__ float4 screen_vertex(float4 c) {
   return make_float4(kSvSpecial, __uint_as_float(m), 0.f, 0.f);
 }
 __device__ __forceinline__ bool sv_normal(float4 s) { return !(fabsf(s.x) > 1.f); }
+
+// ObjectToWorldPos (IShader.h:63-65) of position i.
+__device__ __forceinline__ float4 world_pos_of(const DView& v, int i) {
+  const float4 p = __ldg(v.p4 + i);
+  const float4 w = mat_vec(v.u.model_matrix, p.x, p.y, p.z, 1.f);
+  return make_float4(w.x, w.y, w.z, 0.f);
+}
+// ObjectToWorldNormal (IShader.h:71-75) = [n, 1] * model_I of normal i, with the intensity
+// of Ground / Toon, saturate(worldN . light_dir) (IShader.cpp:8, :26), in w.
+__device__ __forceinline__ float4 world_normal_of(const DView& v, int i) {
+  const float4 n = __ldg(v.n4 + i);
+  const float* m = v.u.model_matrix_I;
+  F3 wn;
+  wn.x = dot4(n.x, n.y, n.z, 1.f, m[0], m[4], m[8], m[12]);
+  wn.y = dot4(n.x, n.y, n.z, 1.f, m[1], m[5], m[9], m[13]);
+  wn.z = dot4(n.x, n.y, n.z, 1.f, m[2], m[6], m[10], m[14]);
+  const F3 L = {v.u.light_dir[0], v.u.light_dir[1], v.u.light_dir[2]};
+  return make_float4(wn.x, wn.y, wn.z, saturate(dot3(wn, L)));
+}
 __device__ __forceinline__ uint32_t sv_mask(float4 s) { return sv_normal(s) ? 0xffu : __float_as_uint(s.y); }
 
 // ---------------------------------------------------------------------------------------
@@ -121,17 +143,15 @@ __device__ __forceinline__ int chunk_view_search(const DView* views, const int32
 struct VchBase { __device__ int32_t operator()(const DView& v) const { return v.vch_base; } };
 struct SchBase { __device__ int32_t operator()(const DView& v) const { return v.sch_base; } };
 
-// Chunk c of the vertex stage: view, kind (0 positions, 1 normals) and item range.
+// Chunk c of the vertex stage: view and position range.
 __device__ __forceinline__ Chunk vertex_chunk(const DView* views, const int32_t* s_base, int nviews, int c) {
   const int k = chunk_view_search(views, s_base, nviews, c, VchBase());
   const DView& v = views[k];
-  int local = c - v.vch_base;
   Chunk ch;
   ch.view = k;
-  ch.kind = local < v.vch_npos ? 0 : 1;
-  if (ch.kind) local -= v.vch_npos;
-  ch.begin = local * kVertexChunk;
-  ch.end = min(ch.kind ? v.nnrm : v.npos, ch.begin + kVertexChunk);
+  ch.kind = 0;
+  ch.begin = (c - v.vch_base) * kVertexChunk;
+  ch.end = min(v.npos, ch.begin + kVertexChunk);
   return ch;
 }
 // Chunk c of the setup stage: view and face range.
@@ -149,58 +169,28 @@ __device__ __forceinline__ Chunk setup_chunk(const DView* views, const int32_t* 
 // ---------------------------------------------------------------------------------------
 // vertex stage
 // ---------------------------------------------------------------------------------------
-// One vertex chunk (kVertexChunk items, 8 per thread, 256 threads).
+// One vertex chunk (kVertexChunk positions, 8 per thread, 256 threads): ObjectToClipPos /
+// ObjectToViewPos (IShader.h:55-61) -> screen vertex.
 __device__ __forceinline__ void vertex_chunk_work(const DView& v, const Chunk& ch) {
   // item i = begin + threadIdx.x + 256 k: consecutive threads read consecutive floats and
   // write consecutive float4s, so every load and store instruction of a warp is one
-  // contiguous span; the four loads of a thread are issued before any is used
+  // contiguous span; the loads of a thread are issued before any is used
   constexpr int kPer = kVertexChunk / 256;
   const int i0 = ch.begin + (int)threadIdx.x;
-  if (ch.kind == 0) {
-    // positions: ObjectToClipPos / ObjectToViewPos (IShader.h:55-61), ObjectToWorldPos (:63-65)
-    float xs[kPer], ys[kPer], zs[kPer];
+  float xs[kPer], ys[kPer], zs[kPer];
 #pragma unroll
-    for (int k = 0; k < kPer; k++) {
-      const int i = i0 + 256 * k;
-      const bool in = i < ch.end;
-      xs[k] = in ? __ldg(v.px + i) : 0.f;
-      ys[k] = in ? __ldg(v.py + i) : 0.f;
-      zs[k] = in ? __ldg(v.pz + i) : 0.f;
-    }
+  for (int k = 0; k < kPer; k++) {
+    const int i = i0 + 256 * k;
+    const bool in = i < ch.end;
+    xs[k] = in ? __ldg(v.px + i) : 0.f;
+    ys[k] = in ? __ldg(v.py + i) : 0.f;
+    zs[k] = in ? __ldg(v.pz + i) : 0.f;
+  }
 #pragma unroll
-    for (int k = 0; k < kPer; k++) {
-      const int i = i0 + 256 * k;
-      if (i >= ch.end) break;
-      v.sv[i] = screen_vertex(mat_vec(v.mvp, xs[k], ys[k], zs[k], 1.f));
-      if (v.wpos) {
-        const float4 w = mat_vec(v.u.model_matrix, xs[k], ys[k], zs[k], 1.f);
-        v.wpos[i] = make_float4(w.x, w.y, w.z, 0.f);
-      }
-    }
-  } else {
-    // normals: ObjectToWorldNormal (IShader.h:71-75) = [n, 1] * model_I; intensity of
-    // Ground/Toon = saturate(worldN . light_dir) (IShader.cpp:8, :26)
-    float xs[kPer], ys[kPer], zs[kPer];
-#pragma unroll
-    for (int k = 0; k < kPer; k++) {
-      const int i = i0 + 256 * k;
-      const bool in = i < ch.end;
-      xs[k] = in ? __ldg(v.nx + i) : 0.f;
-      ys[k] = in ? __ldg(v.ny + i) : 0.f;
-      zs[k] = in ? __ldg(v.nz + i) : 0.f;
-    }
-    const float* m = v.u.model_matrix_I;
-    const F3 L = {v.u.light_dir[0], v.u.light_dir[1], v.u.light_dir[2]};
-#pragma unroll
-    for (int k = 0; k < kPer; k++) {
-      const int i = i0 + 256 * k;
-      if (i >= ch.end) break;
-      F3 wn;
-      wn.x = dot4(xs[k], ys[k], zs[k], 1.f, m[0], m[4], m[8], m[12]);
-      wn.y = dot4(xs[k], ys[k], zs[k], 1.f, m[1], m[5], m[9], m[13]);
-      wn.z = dot4(xs[k], ys[k], zs[k], 1.f, m[2], m[6], m[10], m[14]);
-      v.wnrm[i] = make_float4(wn.x, wn.y, wn.z, saturate(dot3(wn, L)));
-    }
+  for (int k = 0; k < kPer; k++) {
+    const int i = i0 + 256 * k;
+    if (i >= ch.end) break;
+    v.sv[i] = screen_vertex(mat_vec(v.mvp, xs[k], ys[k], zs[k], 1.f));
   }
 }
 
@@ -528,14 +518,14 @@ __device__ __forceinline__ void face_payload(const DView& v, int f, int nf4, Pay
   int4 it = iv, in = iv;  // meshes whose v, vt and vn indices agree skip two loads
   if (!v.unified) {
     if (v.uv && nf4 >= 3) it = __ldg(&v.fvt[f]);
-    if (v.wnrm) in = __ldg(&v.fvn[f]);
+    if (v.world & kWorldNormal) in = __ldg(&v.fvn[f]);
   }
   const int pi[3] = {iv.x, iv.y, iv.z}, ti[3] = {it.x, it.y, it.z}, ni[3] = {in.x, in.y, in.z};
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     const float4 s = __ldg(&v.sv[pi[k]]);
-    const float4 wp = v.wpos ? __ldg(&v.wpos[pi[k]]) : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 wn = v.wnrm ? __ldg(&v.wnrm[ni[k]]) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 wp = (v.world & kWorldPos) ? world_pos_of(v, pi[k]) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 wn = (v.world & kWorldNormal) ? world_normal_of(v, ni[k]) : make_float4(0.f, 0.f, 0.f, 0.f);
     const float2 t = (v.uv && nf4 >= 3) ? __ldg(&v.uv[ti[k]]) : make_float2(0.f, 0.f);
     // recip_w (graphics.cpp:333-337): from the screen vertex, or divided here for a visible
     // vertex with w < 1e-5 (the only kind of special vertex a fast-accepted face can have)
@@ -622,8 +612,8 @@ __device__ void clip_face(const DView& v, int view, int face, int T, const Scrat
     float* o = A + lane * kPolyStride;
     const float4 c = clip_of(v, pi);
     o[0] = c.x; o[1] = c.y; o[2] = c.z; o[3] = c.w;
-    const float4 wp = v.wpos ? v.wpos[pi] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 wn = v.wnrm ? v.wnrm[ni] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 wp = (v.world & kWorldPos) ? world_pos_of(v, pi) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 wn = (v.world & kWorldNormal) ? world_normal_of(v, ni) : make_float4(0.f, 0.f, 0.f, 0.f);
     const float2 t = v.uv ? __ldg(&v.uv[ti]) : make_float2(0.f, 0.f);
     o[4] = wp.x; o[5] = wp.y; o[6] = wp.z;
     o[7] = wn.x; o[8] = wn.y; o[9] = wn.z;

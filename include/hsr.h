@@ -348,7 +348,8 @@ typedef struct hsr_timing {
   uint64_t bin_pairs;      /* (triangle, tile) pairs                                   */
   uint64_t faces;          /* faces processed                                          */
   uint64_t vertices;       /* positions transformed                                    */
-  uint64_t normals;        /* normals transformed                                      */
+  uint64_t normals;        /* normals transformed once per normal (0: world normals are
+                              transformed per corner of the triangles that survive setup) */
   uint64_t clipped_faces;  /* faces that went through the homogeneous clipper          */
   uint64_t fragments;      /* covered (pixel, triangle) pairs tested against the depth  */
   uint64_t raster_pixels;  /* pixels of the tiles the raster visited (tiles with triangles;
