@@ -118,6 +118,25 @@ def test_server_mix_equals_alone(gpu, rp):
         assert np.array_equal(res["outputs"][i], exp["color"]), i
 
 
+def test_long_running_server_across_calls_equals_alone(gpu, rp):
+    """One server and output ring serve two streams in turn (small requests first, then larger
+    ones, so its scratch grows between batches while earlier batches' copies may still run on
+    their slots' streams): every request still equals the same request drawn alone."""
+    small = small_requests(rp.pool, 12, seed=8, max_side=200)
+    large = small_requests(rp.pool, 12, seed=9, max_side=900)
+    srv = gpu.Server(1 << 30, max_batch=6, slots=2)
+    ring = hserve.PinnedRing(64 << 20)
+    try:
+        runs = [hserve.serve_batched(rp, reqs, server=srv, ring=ring, keep_outputs=True) for reqs in (small, large)]
+    finally:
+        srv.close()
+        ring.release()
+    for reqs, res in zip((small, large), runs):
+        assert res["ok"], res["status"]
+        for i, r in enumerate(reqs):
+            assert np.array_equal(res["outputs"][i], alone(rp, r)["color"]), i
+
+
 def serve_all_planes(gpu, rp, reqs, max_batch, slots):
     """Submit every request at once and return colour / depth / prim ids of each."""
     srv = gpu.Server(1 << 30, max_batch=max_batch, slots=slots)
