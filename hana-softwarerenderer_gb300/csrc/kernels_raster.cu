@@ -42,8 +42,8 @@ __device__ __forceinline__ int find_view(const DView* views, const int32_t* tbas
   return lo;
 }
 
-// Wait until every non-empty tile of view `dep` is done (its empty tiles were cleared by
-// k_clear_empty, which runs before the raster).
+// Wait until every non-empty tile of view `dep` is done (its empty tiles were cleared in the
+// scatter grid, which runs before the raster).
 __device__ __forceinline__ void wait_view(const Scratch& sc, const DView* views, int dep) {
   if (dep < 0) return;
   const int tb = views[dep].tile_base;
@@ -169,8 +169,8 @@ __device__ __forceinline__ uint32_t shade_tile(const DView& v, const Scratch& sc
   return shaded;
 }
 
-// One warp per non-empty screen tile (k_scan lists them in tile order; k_clear_empty has
-// written the others).  For each batch of 32 records of the tile list, every record's
+// One warp per non-empty screen tile (k_scan lists them in tile order; the scatter grid has
+// cleared the others).  For each batch of 32 records of the tile list, every record's
 // bounding-box pixels inside the tile form a run of candidates; the non-empty runs are
 // compacted and laid end to end (warp prefix sum) and the lanes walk the candidates 32 at
 // a time, so the work is proportional to the pixels the triangles can touch rather than
