@@ -173,7 +173,13 @@ struct Scratch {
   uint32_t* bins;   uint32_t bin_cap;
   int32_t ntiles;
   int32_t nviews;
+  float* stash;             // [stash_warps][kStashFloats] per raster warp (may be null)
+  uint32_t stash_warps;
 };
+// Per raster warp of a 16x16 tile: the winner's weights b0, b1, b2, payload index and
+// submission per pixel (what shading would otherwise re-derive from the record).
+constexpr int kStashFloats = 5 * 256;
+constexpr int kStashWarpsPerSm = 32;  // raster warps resident per SM at most
 
 // Kernel launchers (kernels_*.cu).  All return cudaError_t as int.
 int launch_vertex(const DView* views, int nviews, int nchunks, int grid, cudaStream_t s);

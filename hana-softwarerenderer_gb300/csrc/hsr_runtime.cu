@@ -184,6 +184,7 @@ int Runtime::plan_build(const hsr_draw_desc* descs, int n, Plan& p) {
   p = Plan();
   p.n = n;
   p.tile = T;
+  p.stash_warps = T == 16 ? (uint32_t)num_sms * kStashWarpsPerSm : 0u;  // 8x8 tiles keep theirs in shared memory
   p.views.resize(n);
   p.offs.resize(n);
   p.order = order;
@@ -285,6 +286,7 @@ void Plan::layout() {
   o_clip = off; off = align_up(off + sizeof(int2) * clip_cap, 256);
   o_big = off; off = align_up(off + sizeof(BigItem) * big_cap, 256);
   o_bins = off; off = align_up(off + sizeof(uint32_t) * bin_cap, 256);
+  o_stash = off; off = align_up(off + sizeof(float) * kStashFloats * (size_t)stash_warps, 256);
   dev_bytes = off;
   stage_bytes = host_bytes + sizeof(Ctl);
 }
@@ -312,6 +314,8 @@ void Plan::bind(char* dev_base, char* host_base) {
   sc.bins = (uint32_t*)(dev + o_bins); sc.bin_cap = (uint32_t)bin_cap;
   sc.ntiles = (int32_t)total_tiles;
   sc.nviews = n;
+  sc.stash = stash_warps ? (float*)(dev + o_stash) : nullptr;
+  sc.stash_warps = stash_warps;
 }
 
 // Upload of the view descriptors, one memset, the kernels, read-back of the control

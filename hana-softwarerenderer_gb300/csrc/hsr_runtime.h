@@ -60,11 +60,12 @@ struct Plan {
   std::vector<DView> views;
   std::vector<Off> offs;
   int nvch = 0, nsch = 0, ncch = 0;  // vertex / setup / clear chunks of the batch (bases in each DView)
+  uint32_t stash_warps = 0;          // raster warps with a stash (the device's SMs x kStashWarpsPerSm)
   size_t view_bytes = 0, total_faces = 0, total_tiles = 0, total_pos = 0, total_nrm = 0, total_pixels = 0;
   size_t rec_cap = 0, clip_cap = 0, bin_cap = 0, big_cap = 0;
   size_t o_views = 0, o_vout = 0, o_zero = 0, zero_bytes = 0, o_ctl = 0, o_done = 0,
          o_cnt = 0, o_fill = 0, o_stat = 0, o_toff = 0, o_neoff = 0, o_list = 0, o_recs = 0, o_pay = 0, o_clip = 0,
-         o_big = 0, o_bins = 0;
+         o_big = 0, o_bins = 0, o_stash = 0;
   size_t dev_bytes = 0, host_bytes = 0, stage_bytes = 0;
   char* dev = nullptr;
   char* host = nullptr;

@@ -87,7 +87,7 @@ struct BatchRecs {
   float ax[32], ay[32], e1x[32], e1y[32], e2x[32], e2y[32], uz[32], d0[32], d1[32], d2[32];
   uint32_t seq[32];    // submission order
   uint32_t idx[32];    // record index
-  uint32_t pay[32];    // payload index (read by tiles that keep the winner's weights)
+  uint32_t pay[32];    // payload index (kept with the winner's weights, in shared memory or the stash)
   uint32_t off[32];    // first candidate of the record's run
   uint32_t box[32];    // box in the tile: x0 | y0 << 8 | width << 16, bit 31 = kRecExact
   uint32_t magic[32];  // ceil(65536 / width): row of a candidate by multiply-shift
@@ -118,11 +118,13 @@ struct TileState {
 
 // Shade the winners of one tile and write colour, depth and prim id (fused clear writes the
 // clear values where nothing won).  S is the shader, known at compile time.  Without kept
-// weights (16x16 tiles) the winner's barycentric weights are evaluated again from its record:
-// the same operations on the same values as in the visibility pass, so the same bits.
+// weights (16x16 tiles) the winner's weights, payload index and submission come from the
+// warp's stash in global memory (written by the visibility pass, read back from L2), or, with
+// no stash, are evaluated again from its record: the same operations on the same values as in
+// the visibility pass either way, so the same bits.
 template <int T, int S>
 __device__ __forceinline__ uint32_t shade_tile(const DView& v, const Scratch& sc, const TileState<T * T>& st, int ox,
-                                               int oy, bool clear, const ByteTables& bt) {
+                                               int oy, bool clear, const ByteTables& bt, const float* stash) {
   constexpr int PPL = T * T / 32;
   constexpr int NF4 = payload_f4_of<S>();
   const int lane = threadIdx.x & 31;
@@ -142,6 +144,12 @@ __device__ __forceinline__ uint32_t shade_tile(const DView& v, const Scratch& sc
         b0 = st.b0[p]; b1 = st.b1[p]; b2 = st.b2[p];
         pay = st.pay[p];
         seq = st.seq[p];
+      } else if (stash) {
+        b0 = __ldcg(stash + p);
+        b1 = __ldcg(stash + 256 + p);
+        b2 = __ldcg(stash + 512 + p);
+        pay = __ldcg(reinterpret_cast<const uint32_t*>(stash) + 768 + p);
+        seq = __ldcg(reinterpret_cast<const uint32_t*>(stash) + 1024 + p);
       } else {
         const RasterRec r = sc.recs[ri];
         cover_test(r.ax, r.ay, r.e1x, r.e1y, r.e2x, r.e2y, r.uz, ((r.view >> kRecFlagShift) & kRecExact) != 0u,
@@ -201,6 +209,11 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
   TileState<NPIX>& st = sst[warp];
   BatchRecs& br = sbr[warp];
   CandQueue& cq = scq[warp];
+  float* stash = nullptr;
+  if constexpr (!TileState<NPIX>::kKeep) {
+    const uint32_t gw = blockIdx.x * (uint32_t)WARPS + (uint32_t)warp;
+    if (sc.stash && gw < sc.stash_warps) stash = sc.stash + (size_t)gw * kStashFloats;
+  }
   if (sc.ctl->error & kErrCapacity) return;
   const uint32_t nrec = min(sc.ctl->rec_count, sc.rec_cap);
 
@@ -299,7 +312,7 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
           br.d0[k] = rr.d0; br.d1[k] = rr.d1; br.d2[k] = rr.d2;
           br.seq[k] = rr.seq;
           br.idx[k] = ri;
-          if constexpr (TileState<NPIX>::kKeep) br.pay[k] = rr.pad;
+          br.pay[k] = rr.pad;
           br.off[k] = start;
           br.box[k] = box | (((rr.view >> kRecFlagShift) & kRecExact) ? 0x80000000u : 0u);
           br.magic[k] = kDivMagic[box >> 16];
@@ -334,6 +347,12 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
               st.b0[p] = b0;
               st.b1[p] = b1;
               st.b2[p] = b2;
+            } else if (stash) {
+              __stcg(stash + p, b0);
+              __stcg(stash + 256 + p, b1);
+              __stcg(stash + 512 + p, b2);
+              __stcg(reinterpret_cast<uint32_t*>(stash) + 768 + p, br.pay[j]);
+              __stcg(reinterpret_cast<uint32_t*>(stash) + 1024 + p, br.seq[j]);
             }
           }
           qh = (qh + cnt) & 63u;
@@ -378,16 +397,16 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
       __syncwarp();
       uint32_t shaded = 0;
       switch (v.shader) {
-        case HSR_SHADER_GROUND: shaded = shade_tile<T, HSR_SHADER_GROUND>(v, sc, st, ox, oy, clear, bt); break;
-        case HSR_SHADER_TOON: shaded = shade_tile<T, HSR_SHADER_TOON>(v, sc, st, ox, oy, clear, bt); break;
-        case HSR_SHADER_TEXTURE: shaded = shade_tile<T, HSR_SHADER_TEXTURE>(v, sc, st, ox, oy, clear, bt); break;
+        case HSR_SHADER_GROUND: shaded = shade_tile<T, HSR_SHADER_GROUND>(v, sc, st, ox, oy, clear, bt, stash); break;
+        case HSR_SHADER_TOON: shaded = shade_tile<T, HSR_SHADER_TOON>(v, sc, st, ox, oy, clear, bt, stash); break;
+        case HSR_SHADER_TEXTURE: shaded = shade_tile<T, HSR_SHADER_TEXTURE>(v, sc, st, ox, oy, clear, bt, stash); break;
         case HSR_SHADER_TEXTURE_WITH_LIGHT:
-          shaded = shade_tile<T, HSR_SHADER_TEXTURE_WITH_LIGHT>(v, sc, st, ox, oy, clear, bt);
+          shaded = shade_tile<T, HSR_SHADER_TEXTURE_WITH_LIGHT>(v, sc, st, ox, oy, clear, bt, stash);
           break;
-        case HSR_SHADER_BLINN: shaded = shade_tile<T, HSR_SHADER_BLINN>(v, sc, st, ox, oy, clear, bt); break;
-        case HSR_SHADER_NORMALMAP: shaded = shade_tile<T, HSR_SHADER_NORMALMAP>(v, sc, st, ox, oy, clear, bt); break;
-        case HSR_SHADER_SHADOW: shaded = shade_tile<T, HSR_SHADER_SHADOW>(v, sc, st, ox, oy, clear, bt); break;
-        default: shaded = shade_tile<T, HSR_SHADER_FLAT>(v, sc, st, ox, oy, clear, bt); break;
+        case HSR_SHADER_BLINN: shaded = shade_tile<T, HSR_SHADER_BLINN>(v, sc, st, ox, oy, clear, bt, stash); break;
+        case HSR_SHADER_NORMALMAP: shaded = shade_tile<T, HSR_SHADER_NORMALMAP>(v, sc, st, ox, oy, clear, bt, stash); break;
+        case HSR_SHADER_SHADOW: shaded = shade_tile<T, HSR_SHADER_SHADOW>(v, sc, st, ox, oy, clear, bt, stash); break;
+        default: shaded = shade_tile<T, HSR_SHADER_FLAT>(v, sc, st, ox, oy, clear, bt, stash); break;
       }
       shaded = __reduce_add_sync(kFull, shaded);
       frags = __reduce_add_sync(kFull, frags);
