@@ -121,7 +121,7 @@ struct __align__(128) DView {
 constexpr int kVertexChunk = 2048;  // positions per vertex-stage chunk
 constexpr uint32_t kWorldPos = 1u, kWorldNormal = 2u;  // DView::world
 constexpr int kSetupChunk = 256;    // faces per setup chunk (one per thread of a block)
-constexpr int kClearChunk = 4096;   // pixels per clear chunk (16 per thread of a block)
+constexpr int kClearChunk = 1024;   // pixels per clear chunk (32 per lane of a warp)
 constexpr int64_t kMaxBatchTiles = (int64_t)1 << 26;  // tiles of one launch sequence (scan word)
 static_assert(offsetof(DView, prim_base) + sizeof(uint32_t) <= 128, "per-tile fields must share one line");
 

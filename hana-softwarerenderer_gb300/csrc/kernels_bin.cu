@@ -186,16 +186,20 @@ __device__ __forceinline__ void scatter_records(const DView* __restrict__ views,
 // The fused clear (renderbuffer_clear_color / renderbuffer_clear_depth, renderbuffer.cpp:59-75,
 // prim ids -> 0) of the pixels whose tile holds no record: the raster visits only the
 // non-empty tiles and writes every pixel of those.  A chunk is kClearChunk consecutive pixels
-// of one view in row-major order, so a warp's stores form one contiguous run per plane; the
-// pixel's tile count (the same word for up to T neighbours) decides whether it is written.
-// Chunks [block, nchunks) in steps of `nblocks`; `cbase` holds the views' chunk bases when
-// the batch has at most kSharedViews views (else null).
+// of one view in row-major order, so a warp's stores form one contiguous run per plane (16 bytes
+// a lane where four neighbours are all cleared); the pixel's tile count (the same word for up
+// to T neighbours) decides whether it is written.
+// Block `block` of the `nblocks` clearing blocks takes chunks warp by warp; `cbase` holds the
+// views' chunk bases when the batch has at most kSharedViews views (else null).
 __device__ __forceinline__ void clear_empty_tiles(const DView* __restrict__ views, int T, int nchunks, const Scratch& sc,
                                                   int block, int nblocks, const int32_t* cbase) {
   if (sc.ctl->error & kErrCapacity) return;  // an overflowing sequence draws nothing
   const int ts = __ffs(T) - 1;
   const int nv = sc.nviews;
-  for (int c = block; c < nchunks; c += nblocks) {
+  const int lane = (int)threadIdx.x & 31, wpb = (int)blockDim.x >> 5;
+  // one chunk per warp at a time: each warp's view lookup and tile counts are an independent
+  // chain of loads, so a block keeps several chunks in flight
+  for (int c = block * wpb + ((int)threadIdx.x >> 5); c < nchunks; c += nblocks * wpb) {
     // the view of chunk c: the last view whose base is <= c (views without chunks share
     // their successor's base and are never the last such view)
     int lo = 0, hi = nv - 1;
@@ -205,32 +209,58 @@ __device__ __forceinline__ void clear_empty_tiles(const DView* __restrict__ view
     }
     const DView& v = views[lo];
     const int W = v.W, npx = v.W * v.H;  // below 2^30 (targets are at most 32768 x 32768)
-    const int i0 = (c - v.cch_base) * kClearChunk + (int)threadIdx.x;
-    const int i1 = min((c - v.cch_base + 1) * kClearChunk, npx);
-    int y = i0 / W, x = i0 - y * W;
-    const int qy = 256 / W, qx = 256 - qy * W;  // the step of 256 pixels in rows and columns
+    const int cbeg = (c - v.cch_base) * kClearChunk, cend = min(cbeg + kClearChunk, npx);
     const int32_t tb = v.tile_base, tx = v.tiles_x;
-    // all of this thread's tile counts in flight at once, then the stores
-    constexpr int kPer = kClearChunk / 256;
-    uint32_t empty = 0;  // bit k: pixel i0 + 256k is in the chunk and its tile has no record
+    // groups of 4 consecutive pixels (a group may run on into the next row): lane l takes the
+    // groups starting at cbeg + 4l + 128k, k < kGroups; all of a lane's tile counts are in
+    // flight before its stores
+    constexpr int kGroups = kClearChunk / 128;
+    const int g0 = cbeg + 4 * lane;
+    int y = g0 / W, x = g0 - y * W;
+    const int qy = 128 / W, qx = 128 - qy * W;  // the step of 128 pixels in rows and columns
+    uint32_t empty = 0;  // bit 4k + d: pixel g0 + 128k + d is in the chunk and its tile has no record
 #pragma unroll
-    for (int k = 0; k < kPer; k++) {
-      if (i0 + 256 * k < i1 && sc.tile_count[tb + (y >> ts) * tx + (x >> ts)] == 0u) empty |= 1u << k;
+    for (int k = 0; k < kGroups; k++) {
+#pragma unroll
+      for (int d = 0; d < 4; d++) {
+        int xx = x + d, yy = y;
+        if (xx >= W) {  // the group runs on into the next row(s)
+          yy += xx / W;
+          xx -= (xx / W) * W;
+        }
+        if (g0 + 128 * k + d < cend && sc.tile_count[tb + (yy >> ts) * tx + (xx >> ts)] == 0u)
+          empty |= 1u << (4 * k + d);
+      }
       x += qx;
       y += qy;
       if (x >= W) { x -= W; y++; }
     }
-    if (!empty) continue;
+    if (!__any_sync(0xffffffffu, empty != 0u)) continue;
     const uint32_t rgba = v.clear_rgba;
     const float depth = v.clear_depth;
     uint32_t* const prim = v.prim;
+    // a group starts at a multiple of 4 pixels, so with 16-byte aligned planes (the library
+    // allocates them 256-byte aligned) a full group is one 16-byte store per plane
+    const bool vec = ((reinterpret_cast<uintptr_t>(v.color) | reinterpret_cast<uintptr_t>(v.depth) |
+                       reinterpret_cast<uintptr_t>(prim)) & 15u) == 0u;
 #pragma unroll
-    for (int k = 0; k < kPer; k++) {
-      if (empty >> k & 1u) {
-        const int i = i0 + 256 * k;
-        v.color[i] = rgba;
-        v.depth[i] = depth;
-        if (prim) prim[i] = 0u;
+    for (int k = 0; k < kGroups; k++) {
+      const uint32_t m = (empty >> (4 * k)) & 15u;
+      if (!m) continue;
+      const int i = g0 + 128 * k;
+      if (m == 15u && vec) {
+        *reinterpret_cast<uint4*>(v.color + i) = make_uint4(rgba, rgba, rgba, rgba);
+        *reinterpret_cast<float4*>(v.depth + i) = make_float4(depth, depth, depth, depth);
+        if (prim) *reinterpret_cast<uint4*>(prim + i) = make_uint4(0u, 0u, 0u, 0u);
+      } else {
+#pragma unroll
+        for (int d = 0; d < 4; d++) {
+          if (m >> d & 1u) {
+            v.color[i + d] = rgba;
+            v.depth[i + d] = depth;
+            if (prim) prim[i + d] = 0u;
+          }
+        }
       }
     }
   }
