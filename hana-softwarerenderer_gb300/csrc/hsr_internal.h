@@ -150,7 +150,6 @@ struct __align__(16) BigItem {
 // Work chunk for the vertex and setup kernels: items [begin, end) of one view.
 struct Chunk {
   int32_t view;
-  int32_t kind;   // vertex kernel: 0 = positions, 1 = normals
   int32_t begin;
   int32_t end;
 };

@@ -149,7 +149,6 @@ __device__ __forceinline__ Chunk vertex_chunk(const DView* views, const int32_t*
   const DView& v = views[k];
   Chunk ch;
   ch.view = k;
-  ch.kind = 0;
   ch.begin = (c - v.vch_base) * kVertexChunk;
   ch.end = min(v.npos, ch.begin + kVertexChunk);
   return ch;
@@ -160,7 +159,6 @@ __device__ __forceinline__ Chunk setup_chunk(const DView* views, const int32_t* 
   const DView& v = views[k];
   Chunk ch;
   ch.view = k;
-  ch.kind = 0;
   ch.begin = (c - v.sch_base) * kSetupChunk;
   ch.end = min(v.nfaces, ch.begin + kSetupChunk);
   return ch;
