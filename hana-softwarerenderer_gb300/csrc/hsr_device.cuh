@@ -117,7 +117,7 @@ __device__ __forceinline__ F3 tex_normal(const DView& v, float u, float t, const
 // e1 = B - A, e2 = C - A and u.z = e2.x*e1.y - e1.x*e2.y (|u.z| > 0.01).  Weights are
 // (1 - (u.x+u.y)/u.z, u.y/u.z, u.x/u.z); the pixel is covered when all three are >= 0.
 // `exact` selects the literal divisions; otherwise the sign test on u.x, u.y, u.x+u.y
-// against u.z decides coverage without dividing (equal to the divisions' verdict for
+// against u.z decides coverage without dividing (equal to the divisions' decision for
 // coordinates in the range setup checks) and the weights are computed only when covered.
 // The raster and the setup-side cull of pixel-less triangles share these functions, so both
 // take the same decision for every pixel.
