@@ -120,6 +120,15 @@ struct __align__(128) DView {
 };
 constexpr int kVertexChunk = 2048;  // positions per vertex-stage chunk
 constexpr uint32_t kWorldPos = 1u, kWorldNormal = 2u;  // DView::world
+// The world attributes a shader's fragment() reads (IShader.cpp): the world position for the
+// view vector and the shadow lookup, the world normal for lighting (and the intensity of
+// Ground / Toon, which rides in its w).
+__host__ __device__ inline uint32_t world_attrs(int shader) {
+  const bool pos = shader == HSR_SHADER_BLINN || shader == HSR_SHADER_NORMALMAP;
+  const bool nrm = shader == HSR_SHADER_GROUND || shader == HSR_SHADER_TOON || shader == HSR_SHADER_TEXTURE_WITH_LIGHT ||
+                   shader == HSR_SHADER_BLINN || shader == HSR_SHADER_NORMALMAP;
+  return (pos ? kWorldPos : 0u) | (nrm ? kWorldNormal : 0u);
+}
 constexpr int kSetupChunk = 256;    // faces per setup chunk (one per thread of a block)
 constexpr int kClearChunk = 1024;   // pixels per clear chunk (32 per lane of a warp)
 constexpr int64_t kMaxBatchTiles = (int64_t)1 << 26;  // tiles of one launch sequence (scan word)

@@ -48,12 +48,6 @@ static void* g_noalloc_dev[kMaxDevices];
 
 static size_t nal(size_t x) { return (x + 255) / 256 * 256; }
 
-static bool needs_wpos_h(int s) { return s == HSR_SHADER_BLINN || s == HSR_SHADER_NORMALMAP; }
-static bool needs_wnrm_h(int s) {
-  return s == HSR_SHADER_GROUND || s == HSR_SHADER_TOON || s == HSR_SHADER_TEXTURE_WITH_LIGHT ||
-         s == HSR_SHADER_BLINN || s == HSR_SHADER_NORMALMAP;
-}
-
 static int noalloc_draw(Runtime* rt, const hsr_draw_desc& d) {
   int rc = rt->validate(d);
   if (rc != HSR_OK) return rc;
@@ -79,7 +73,7 @@ static int noalloc_draw(Runtime* rt, const hsr_draw_desc& d) {
   v.px = m->px; v.py = m->py; v.pz = m->pz;
   v.nx = m->nx; v.ny = m->ny; v.nz = m->nz;
   v.p4 = m->p4; v.n4 = m->n4;
-  v.world = (needs_wpos_h(d.shader) ? kWorldPos : 0u) | (needs_wnrm_h(d.shader) ? kWorldNormal : 0u);
+  v.world = world_attrs(d.shader);
   v.uv = m->uv;
   v.fv = m->fv; v.fvt = m->fvt; v.fvn = m->fvn;
   v.npos = m->npos; v.nnrm = m->nnrm; v.nuv = m->nuv; v.nfaces = m->nfaces;

@@ -118,12 +118,6 @@ TexObj* Runtime::tex(uint64_t h) { return get(textures, h); }
 TargetObj* Runtime::target(uint64_t h) { return get(targets, h); }
 
 // ---- batch planning -----------------------------------------------------------------------
-static bool shader_needs_wpos(int s) { return s == HSR_SHADER_BLINN || s == HSR_SHADER_NORMALMAP; }
-static bool shader_needs_wnrm(int s) {
-  return s == HSR_SHADER_GROUND || s == HSR_SHADER_TOON || s == HSR_SHADER_TEXTURE_WITH_LIGHT ||
-         s == HSR_SHADER_BLINN || s == HSR_SHADER_NORMALMAP;
-}
-
 int Runtime::validate(const hsr_draw_desc& d) {
   if (!d.uniforms) return fail(HSR_ERR_INVALID_ARG, "draw: uniforms is null");
   if (d.shader < 0 || d.shader >= HSR_SHADER_COUNT) return fail(HSR_ERR_UNKNOWN_SHADER, "draw: unknown shader kind");
@@ -198,7 +192,7 @@ int Runtime::plan_build(const hsr_draw_desc* descs, int n, Plan& p) {
     v.px = m->px; v.py = m->py; v.pz = m->pz;
     v.nx = m->nx; v.ny = m->ny; v.nz = m->nz;
     v.p4 = m->p4; v.n4 = m->n4;
-    v.world = (shader_needs_wpos(d.shader) ? kWorldPos : 0u) | (shader_needs_wnrm(d.shader) ? kWorldNormal : 0u);
+    v.world = world_attrs(d.shader);
     v.uv = m->uv;
     v.fv = m->fv; v.fvt = m->fvt; v.fvn = m->fvn;
     v.npos = m->npos; v.nnrm = m->nnrm; v.nuv = m->nuv; v.nfaces = m->nfaces;
