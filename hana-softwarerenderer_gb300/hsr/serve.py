@@ -93,8 +93,10 @@ class PinnedRing:
     reused only after the request that owns it has completed.  Allocation and release are
     O(1): regions are handed out and reclaimed first in, first out."""
 
-    def __init__(self, nbytes: int):
-        self.buf = PinnedArray((nbytes,), np.uint8)
+    def __init__(self, nbytes: int, buffer=None):
+        """`buffer`: an object with `.array` (nbytes uint8) and `.release()`; page-locked memory
+        from the library when omitted."""
+        self.buf = buffer if buffer is not None else PinnedArray((nbytes,), np.uint8)
         self.cap = nbytes
         self.head = 0                                     # next free byte
         self.live: collections.deque = collections.deque()  # [key, start, end, freed] in allocation order
