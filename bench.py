@@ -22,8 +22,9 @@ plain_per_frame   the same requests one at a time through the per-frame drop-in 
 serve     10,000 Poisson arrivals at two offered loads (80% of the plain path's capacity and
           80% of the server's): frames/s and p50 / p99 latency from scheduled arrival, for
           the server and for the plain path.
-roofline  the kernel with the largest share of the batched step: algorithmic bytes per
-          launch / its CUDA-event duration, against the measured HBM copy bandwidth.
+roofline  every kernel of the batched step: algorithmic bytes per launch / its CUDA-event
+          duration, against the measured HBM copy bandwidth; the headline is the kernel with
+          the largest share.
 frame_1080p / batched_views_64   the single 1080p frame and the 64-view batched launch.
 cpu_baseline  the oracle (C restatement of the reference) on this host's cores, bounded
           sample of the same request stream.
@@ -58,6 +59,8 @@ FRAME_WORKLOAD = ("displaced icosphere-7 (327,680 tris) + 2-tri ground plane, 19
 SOUP_WORKLOAD = ("triangle soup, 4,000,000 tris at 3840x2160, centroids uniform, lognormal edges (median 2 px), "
                  "constant NDC depth U[0,1] (~8x depth complexity), 1% exact duplicates submitted later, flat shader")
 BATCH = 64          # requests per launch sequence (the server's max_batch)
+COUNT_KEYS = ("faces", "vertices", "normals", "records", "bin_pairs", "pixels", "shaded_pixels", "clipped_faces",
+              "raster_pixels", "fragments", "tiles", "split_triangles", "payload_bytes")
 N_REQUESTS = 10000  # Poisson stream length
 SEED = 5
 
@@ -158,31 +161,39 @@ def dist_barrier(world: int):
 
 
 def kernel_bytes(t: dict) -> dict:
-    """Algorithmic bytes per launch of each kernel of one launch sequence.
+    """Algorithmic bytes per launch of each kernel of one launch sequence (the floor a kernel
+    must move to or from HBM; intermediate results the design keeps in L2 still count).
 
-    vertex : 12 B read + 16 B screen vertex written per position (world positions and
-             normals are transformed per corner of the surviving triangles, in the setup
-             segment).
-    setup  : 16 B index read + 16 B clip read per face corner set (each vertex once) + a
-             64 B record written per triangle that reaches the raster.
-    scan   : 4 B read + 4 B written per tile.
+    vertex : 12 B position read + 16 B screen vertex written per position.
+    cull   : 16 B face indices per face + 16 B screen vertex per position (each gathered
+             once) + a 64 B record written per triangle that reaches the raster.
+    emit   : per surviving triangle 32 B of its record and 16 B face indices read, a 4 B
+             payload index written, and the shading payload written (payload_bytes, counted
+             by the kernels: 0-128 B by shader); the position, normal, uv and screen vertex
+             (56 B) of each vertex of a surviving triangle read once, records / 2 vertices
+             (a closed triangle mesh has half as many vertices as faces).
+    clip   : per clipped face 48 B of indices and 3 x 56 B of corner attributes.
+    split  : per split triangle its 192 B queue entry read.
+    scan   : 4 B read + 12 B written per tile (offset, non-empty prefix, list entry).
     scatter: 16 B of each record read + 4 B written per (triangle, tile) pair, and the fused
              clear of the tiles without triangles: 12 B written per pixel (colour, depth,
              prim id) outside the raster's tiles.
-    raster : 12 B written per pixel of the tiles it visits (colour, depth, prim id), 4 B read
-             per (triangle, tile) pair + the 64 B record, and per shaded pixel the texels it
-             samples (diffuse, normal map, shadow map: 4 B each) — vertex attributes of the
-             visible triangles are counted once per record (3 corners x 56 B).
+    raster : 12 B written per pixel of the tiles it visits, 4 B read per (triangle, tile)
+             pair, the 64 B record and the shading payload of each triangle, and one 4 B
+             texel per shaded pixel (the diffuse map; normal and shadow maps not counted).
     """
     px, rec, pairs = t["pixels"], t["records"], t["bin_pairs"]
     rpx = t.get("raster_pixels", px)
-    tiles = px / 64.0  # tiles of the scan, counted as 8x8 (the 16x16 grid has fewer)
+    pay = t.get("payload_bytes", rec * 128)
     return {
         "vertex": t["vertices"] * 28 + t["normals"] * 28,
-        "setup": t["faces"] * 16 + t["vertices"] * 16 + rec * 64,
-        "scan": tiles * 8,
+        "cull": t["faces"] * 16 + t["vertices"] * 16 + rec * 64,
+        "emit": rec * 52 + pay + (rec // 2) * 56,
+        "clip": t["clipped_faces"] * (48 + 3 * 56),
+        "split": t.get("split_triangles", 0) * 192,
+        "scan": t.get("tiles", px / 64.0) * 16,
         "scatter": rec * 16 + pairs * 4 + (px - rpx) * 12,
-        "raster": rpx * 12 + pairs * 4 + rec * (64 + 3 * 56) + t["shaded_pixels"] * 12,
+        "raster": rpx * 12 + pairs * 4 + rec * 64 + pay + t["shaded_pixels"] * 4,
     }
 
 
@@ -196,22 +207,27 @@ def ncu_traffic(workload: str, kernel: str):
     return d.get("workloads", {}).get(workload, {}).get("dram_bytes_per_launch", {}).get(kernel)
 
 
-# The setup segment of hsr_last_timing spans four kernels (k_setup, k_emit, k_post, k_big); the
-# roofline is reported for the largest segment that is one kernel.
-SINGLE_KERNEL_SEGMENTS = ("vertex", "scan", "scatter", "raster")
-
-
 def roofline(kernel_ms: dict, counts: dict, workload: str) -> dict:
+    """The kernel with the largest share of the launch sequence, against the measured HBM
+    copy bandwidth, and every kernel's own figures beside it."""
     mean_k = {k: statistics.mean(v) for k, v in kernel_ms.items()}
-    top = max((k for k in mean_k if k in SINGLE_KERNEL_SEGMENTS), key=mean_k.get)
     kb = kernel_bytes(counts)
     pk = peaks()
-    achieved = kb[top] / (mean_k[top] * 1e-3) / 1e9
-    return {"kernel": top, "bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"],
-            "peak_source": pk["source"], "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4),
-            "algorithmic_bytes": int(kb[top]), "ms": round(mean_k[top], 5), "traffic": ncu_traffic(workload, top),
-            "share": {k: round(v / sum(mean_k.values()), 4) for k, v in mean_k.items()},
-            "note": "largest single-kernel segment; setup = k_setup + k_emit + k_post + k_big"}
+    total = sum(mean_k.values())
+    per = {}
+    for k, ms in mean_k.items():
+        gbs = kb[k] / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
+        per[k] = {"ms": round(ms, 5), "share": round(ms / total, 4) if total else 0.0,
+                  "algorithmic_bytes": int(kb[k]), "achieved_gbs": round(gbs, 1),
+                  "frac": round(gbs / pk["hbm_gbs"], 4), "traffic": ncu_traffic(workload, k)}
+    top = max(mean_k, key=mean_k.get)
+    return {"kernel": top, "bound": "hbm", "achieved": per[top]["achieved_gbs"], "peak": pk["hbm_gbs"],
+            "peak_source": pk["source"], "unit": "GB/s", "frac": per[top]["frac"],
+            "algorithmic_bytes": per[top]["algorithmic_bytes"], "ms": per[top]["ms"], "traffic": per[top]["traffic"],
+            "kernels": per,
+            "note": "the kernel with the largest share of the step; every kernel's share, algorithmic bytes and "
+                    "fraction of the measured copy bandwidth under 'kernels' (the raster is issue-bound: its "
+                    "issue and FP32-pipe figures are in profiles/)"}
 
 
 def serve_inputs(n: int):
@@ -279,8 +295,7 @@ def run_ours(args, world, rank, local):
         launches += int(t["launches"])
         h2d.append(int(t["h2d_bytes"]))
         d2h.append(sum(r.width * r.height * 4 for r in chunk) + int(t["d2h_bytes"]))
-        for k in ("faces", "vertices", "normals", "records", "bin_pairs", "pixels", "shaded_pixels", "clipped_faces",
-                  "raster_pixels"):
+        for k in COUNT_KEYS:
             counts_sum[k] = counts_sum.get(k, 0) + int(t[k])
     torch.cuda.synchronize()
     clocks = sampler.stop()
@@ -347,12 +362,19 @@ def run_ours(args, world, rank, local):
             "note": "same requests, all at t=0, one at a time: hsr_target_create x2, hsr_draw_batch (shadow + "
                     "main), hsr_target_download (colour), hsr_target_release x2; wall clock"}
         out["serve"] = serve_poisson(rp, reqs, plain_fps, e2e["value"], args)
+        at = out["serve"]["load_server80"]
+        e2e["poisson_at_server_load"] = {
+            "rate_per_s": at["rate_per_s"], "server_p50_ms": at["server"]["p50_ms"],
+            "server_p99_ms": at["server"]["p99_ms"], "plain_p50_ms": at["plain"]["p50_ms"],
+            "plain_p99_ms": at["plain"]["p99_ms"],
+            "note": "10,000 Poisson arrivals at 80% of the server's measured capacity; latency from each "
+                    "request's scheduled arrival to its colour on the host"}
         out["frame_1080p"] = run_frame(args)
         out["batched_views_64"] = run_views(args)
         out["depth_stress_4m"] = run_soup(args)
     rp.release()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(pool, tex, reqs, args.cpu_seconds)
+        out["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
     out["gen_s"] = round(gen_s, 2)
     return out
 
@@ -410,8 +432,7 @@ def run_frame(args) -> dict:
         g.render(batched=False)
         plain.append((time.perf_counter() - s0) * 1000.0)
     hsr.set_profiling(False)
-    counts = {k: int(t[k]) for k in ("faces", "vertices", "normals", "records", "bin_pairs", "pixels",
-                                     "shaded_pixels", "clipped_faces", "raster_pixels")}
+    counts = {k: int(t[k]) for k in COUNT_KEYS}
     res = {"workload": FRAME_WORKLOAD, "frames_per_s": round(1000.0 / statistics.mean(ms), 2),
            "ms_p50": round(float(np.percentile(ms, 50)), 4), "ms_p99": round(float(np.percentile(ms, 99)), 4),
            "plain_two_draw_calls_frames_per_s": round(1000.0 / statistics.mean(plain), 2),
@@ -450,8 +471,7 @@ def run_soup(args) -> dict:
         for k, v in t["kernel_ms"].items():
             kms[k].append(v)
     hsr.set_profiling(False)
-    counts = {k: int(t[k]) for k in ("faces", "vertices", "normals", "records", "bin_pairs", "pixels",
-                                     "shaded_pixels", "fragments", "clipped_faces", "raster_pixels")}
+    counts = {k: int(t[k]) for k in COUNT_KEYS}
     s = statistics.mean(ms) / 1000.0
     res = {"workload": SOUP_WORKLOAD, "frames_per_s": round(1.0 / s, 2), "ms": round(s * 1000.0, 4),
            "mtris_per_s": round(counts["faces"] / s / 1e6, 1),
@@ -513,62 +533,69 @@ def run_views(args) -> dict:
 
 
 # ------------------------------------------------------------------------------------------
-# CPU: the oracle on a bounded sample of the same request stream
+# CPU: the oracle (C restatement of the reference's path) on this host's cores
 # ------------------------------------------------------------------------------------------
-def cpu_render_requests(pool, tex, reqs, threads: int, seconds: float | None = None) -> tuple:
-    """`threads` threads render `reqs` in order, one request per task; with `seconds`, no
-    task starts after that much wall time.  Returns (requests rendered, wall seconds)."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
+def _serve_seeds() -> dict:
+    """What a worker process needs to rebuild the serving workload (serve_inputs)."""
     from hsr import scenes
 
-    lock = threading.Lock()
-    nxt = [0]
-    done = [0]
-    s0 = time.perf_counter()
-
-    def worker():
-        while True:
-            with lock:
-                i = nxt[0]
-                if i >= len(reqs) or (seconds is not None and time.perf_counter() - s0 >= seconds):
-                    return
-                nxt[0] += 1
-            oracle.render_frame(scenes.view_frame(reqs[i], pool, tex))
-            with lock:
-                done[0] += 1
-
-    ths = [threading.Thread(target=worker) for _ in range(threads)]
-    for t in ths:
-        t.start()
-    for t in ths:
-        t.join()
-    return done[0], time.perf_counter() - s0
+    return {"pool_spec": scenes.SERVE_POOL_SPEC, "pool_seed": 1, "ntex": 4, "tex_size": 1024, "tex_seed": 17,
+            "nreq": N_REQUESTS, "req_seed": SEED}
 
 
-def cpu_baseline(pool, tex, reqs, seconds: float, threads: int | None = None) -> dict:
-    threads = threads or os.cpu_count() or 1
-    n, s = cpu_render_requests(pool, tex, reqs, threads, seconds)
-    return {"value": round(n / s, 4), "unit": "frames/s", "cores": threads, "kind": "port",
-            "sample": f"the first {n} requests of the serving stream, {threads} threads, {s:.1f} s wall "
-                      f"(no request starts after {seconds:.0f} s)"}
+def _process_renderer(procs: int):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import cpu_runner
+
+    return cpu_runner.ProcessRenderer(procs, **_serve_seeds())
+
+
+def cpu_latency() -> dict:
+    """The reference path's single-frame latency on one core (one frame at a time): the plain
+    512x512 frame, the 1920x1080 + 2048^2 shadow frame and the 4M-triangle soup."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import cpu_runner
+    from hsr import scenes
+
+    frames = {"plain_512": scenes.sphere_frame(4, 512, 512, seed=1), "frame_1080p": scenes.displaced_frame(),
+              "soup_4m_2160p": scenes.soup_frame()}
+    return cpu_runner.latency(frames, {"plain_512": 40, "frame_1080p": 6, "soup_4m_2160p": 3})
+
+
+def cpu_baseline(seconds: float) -> dict:
+    """Throughput: one oracle process per host core on the serving stream (independent
+    processes, each taking the next request as it frees up; no request starts after
+    `seconds`); latency: single frames on one core."""
+    procs = os.cpu_count() or 1
+    pr = _process_renderer(procs)
+    try:
+        n, s = pr.render_for(range(N_REQUESTS), seconds)
+    finally:
+        pr.close()
+    return {"value": round(n / s, 4), "unit": "frames/s", "cores": procs, "kind": "port",
+            "sample": f"the first {n} requests of the serving stream on {procs} independent processes (one per "
+                      f"core), {s:.1f} s wall, no request started after {seconds:.0f} s",
+            "latency_1core": cpu_latency()}
 
 
 def run_reference(args, world, rank):
-    """The reference's CPU implementation of the path with every host thread, on the same
-    request stream: each step renders the next 64 requests (one step of ours), the threads
-    taking requests as they free up."""
+    """The reference's CPU implementation of the path (the oracle port) on every host core, on
+    the same request stream: one process per core, each step the next 64 requests, each
+    request taken by whichever process frees up first."""
     if rank != 0:
         return None
-    pool, tex, reqs = serve_inputs(N_REQUESTS)
-    threads = os.cpu_count() or 1
+    procs = os.cpu_count() or 1
+    pr = _process_renderer(procs)
     pos = 0
     secs = []
-    for i in range(args.warmup + args.steps):
-        n, s = cpu_render_requests(pool, tex, reqs[pos:pos + BATCH], threads)
-        pos = (pos + BATCH) % (len(reqs) - BATCH)
-        if i >= args.warmup:
-            secs.append(s)
+    try:
+        for i in range(args.warmup + args.steps):
+            s, _ = pr.render(range(pos, pos + BATCH))
+            pos = (pos + BATCH) % (N_REQUESTS - BATCH)
+            if i >= args.warmup:
+                secs.append(s)
+    finally:
+        pr.close()
     value = args.steps * BATCH / sum(secs)
     per = [s * 1000.0 for s in secs]
     return {
@@ -576,8 +603,9 @@ def run_reference(args, world, rank):
         "warmup": args.warmup, "ms_per_step": round(statistics.mean(per), 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
         "config": {"workload": SERVE_WORKLOAD, "frames_per_step": BATCH, "l2": "n/a (host)"},
-        "cpu_baseline": {"value": round(value, 4), "unit": "frames/s", "cores": threads, "kind": "port",
-                         "sample": f"{BATCH} distinct requests per step on {threads} threads, {args.steps} steps"},
+        "cpu_baseline": {"value": round(value, 4), "unit": "frames/s", "cores": procs, "kind": "port",
+                         "sample": f"{BATCH} distinct requests per step on {procs} independent processes (one per "
+                                   f"core), {args.steps} steps"},
         "e2e": {"value": round(value, 4), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gpu_launches": 0,
     }

@@ -40,6 +40,12 @@ enum : uint32_t {
   kErrBigOverflow = 32u,
 };
 constexpr uint32_t kErrCapacity = kErrRecOverflow | kErrClipOverflow | kErrBinOverflow | kErrBigOverflow;
+// A sequence with one of these draws nothing: the binning and the raster return before
+// writing (an overflow is re-run with larger scratch; a scan that gave up has no tile lists).
+constexpr uint32_t kErrNoDraw = kErrCapacity | kErrScanTimeout;
+// Default poll limits of the bounded waits (Scratch::poll_limit overrides both).
+constexpr long kDepWaitPolls = 1L << 23;   // raster: a shadow map's tiles (~1-2 s)
+constexpr long kScanWaitPolls = 1L << 22;  // scan: a predecessor block's prefix
 
 // Record flags.
 enum : uint32_t {
@@ -147,7 +153,9 @@ struct Ctl {
   unsigned long long frag_px;    // covered (pixel, triangle) pairs the raster depth-tested
   uint32_t ne_tiles;             // tiles with at least one record (k_scan)
   uint32_t ctl_pad;
+  unsigned long long pay_bytes;  // shading payload bytes written (k_emit, k_post, k_big)
 };
+static_assert(sizeof(Ctl) == 64, "Ctl is read back whole: keep it one 64-byte block");
 
 // A triangle whose bounding box touches more than kMaxRecordTiles tiles, queued by setup
 // and expanded into sub-records by k_post.
@@ -183,6 +191,8 @@ struct Scratch {
   int32_t nviews;
   float* stash;             // [stash_warps][kStashFloats] per raster warp (may be null)
   uint32_t stash_warps;
+  uint32_t faults;          // HSR_FAULT_* injected by the host (tests of the failure paths)
+  int32_t poll_limit;       // polls before a bounded wait gives up (0: the defaults above)
 };
 // Per raster warp of a 16x16 tile: the winner's weights b0, b1, b2, payload index and
 // submission per pixel (what shading would otherwise re-derive from the record).

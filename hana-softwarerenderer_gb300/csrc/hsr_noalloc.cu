@@ -2,14 +2,14 @@
 //
 // hsr_draw() sizes its scratch (view descriptors, transformed vertices, triangle records,
 // tile lists) per call and grows a device arena and a page-locked staging buffer with
-// cudaMalloc / cudaMallocHost when a draw needs more.  Some callers cannot allow that:
-// code that records its work into a CUDA graph (allocation is not permitted while a stream
-// is being captured), real-time loops that must not stall on the device-wide
-// synchronisation cudaMalloc implies, and processes that run under a fixed device-memory
-// budget.  hsr_draw_noalloc() renders the same draw with the same kernels, but its scratch
-// is one file-scope __device__ array of kStaticScratchBytes (128 MiB) and its host-side
-// staging is a file-scope host array: it calls no cudaMalloc, cudaFree, cudaMallocHost or
-// other allocating routine.
+// cudaMalloc / cudaMallocHost when a draw needs more.  Some callers cannot allow that: render
+// loops with a frame deadline (allocating or freeing device memory can synchronise the whole
+// device), processes held to a fixed device-memory budget that must not grow once running
+// (a GPU shared with other services, where a late allocation can fail mid-frame), and host
+// applications that forbid allocation inside their per-frame callbacks.  hsr_draw_noalloc()
+// renders the same draw with the same kernels, but its scratch is one file-scope __device__
+// array of kStaticScratchBytes (128 MiB) and its host-side staging is a file-scope host
+// array: it calls no cudaMalloc, cudaFree, cudaMallocHost or other allocating routine.
 //
 // Limits and sharing:
 //   - the success path allocates nothing on the device or the host (a failing call only
@@ -18,11 +18,14 @@
 //     (roughly 400k faces into a 1920x1080 target); one that overflows it on the device
 //     (more clipped or large triangles than the fixed split allows) returns
 //     HSR_ERR_BIN_OVERFLOW and leaves the target untouched;
+//   - the call is synchronous: it runs on the library's stream and waits for its own result;
 //   - every GPU that loads libhsr holds the array until the process exits;
-//   - all calls share the array; each call clears the counters it needs, but two calls
-//     whose work overlaps on the GPU race on the array: run them one after another;
+//   - all calls share the array, which keeps the last call's contents; each call clears the
+//     counters it needs, but two calls whose work overlaps on the GPU race on the array: run
+//     them one after another;
 //   - the first call on a device looks up the array's device address (cudaGetSymbolAddress)
-//     for that device; make that first call before any stream capture.
+//     for that device, with that device current; make that first call before any stream
+//     capture begins.
 #include <cuda_runtime.h>
 
 #include <algorithm>

@@ -314,39 +314,48 @@ void Plan::bind(char* dev_base, char* host_base) {
 
 // Upload of the view descriptors, one memset, the kernels, read-back of the control
 // block: everything stream-ordered, nothing synchronous (capturable into a CUDA graph).
+// `ev` (may be null) holds Runtime::kEvents events: [0] before the upload and [kEvents-1]
+// after the raster are recorded whenever `ev` is given; [1] after the memset and [2+k]
+// after kernel k only where non-null (profiling).
 int Plan::enqueue(cudaStream_t s, int num_sms, const hsr_tuning& tu, cudaEvent_t* ev) {
   const DView* dviews = (const DView*)(dev + o_views);
-  if (ev) cudaEventRecord(ev[0], s);
+  auto mark = [&](int k) {
+    if (ev && ev[k]) cudaEventRecord(ev[k], s);
+  };
+  mark(0);
   cudaError_t e = cudaMemcpyAsync(dev, host, host_bytes, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "upload views");
   e = cudaMemsetAsync(dev + o_zero, 0, zero_bytes, s);
   if (e != cudaSuccess) return cuda_fail(e, "clear scratch");
-  if (ev && ev[1]) cudaEventRecord(ev[1], s);
+  mark(1);
   int kr = launch_vertex(dviews, n, nvch, num_sms * 8, s);
   if (kr) return cuda_fail((cudaError_t)kr, "vertex kernel");
-  if (ev && ev[2]) cudaEventRecord(ev[2], s);
+  mark(2);
   kr = launch_setup(dviews, n, nsch, sc, num_sms * 4, s);
   if (kr) return cuda_fail((cudaError_t)kr, "setup kernel");
+  mark(3);
   kr = launch_emit(dviews, tile, sc, num_sms * 8, s);
   if (kr) return cuda_fail((cudaError_t)kr, "emit kernel");
+  mark(4);
   kr = launch_post(dviews, tile, sc, num_sms * 4, s);
   if (kr) return cuda_fail((cudaError_t)kr, "post kernel");
+  mark(5);
   kr = launch_big(dviews, tile, sc, num_sms * 2, s);
   if (kr) return cuda_fail((cudaError_t)kr, "big-triangle kernel");
-  if (ev && ev[3]) cudaEventRecord(ev[3], s);
+  mark(6);
   kr = launch_scan(sc, s);
   if (kr) return cuda_fail((cudaError_t)kr, "scan kernel");
-  if (ev && ev[4]) cudaEventRecord(ev[4], s);
-  // grid-stride over the records: a full-occupancy grid, not one sized by the capacity
-  // (which can be far above this batch's record count)
-  // one full wave of 256-thread blocks (fewer when there are few records and nothing to clear)
+  mark(7);
+  // grid-stride over the records: one full wave of 256-thread blocks (fewer when there are
+  // few records and nothing to clear), not one sized by the capacity (which can be far
+  // above this batch's record count)
   const size_t want = ncch ? (size_t)num_sms * 8 : std::min<size_t>((rec_cap + 255) / 256, (size_t)num_sms * 8);
   kr = launch_scatter(dviews, tile, sc, (int)std::max<size_t>(want, 1), ncch, s);
   if (kr) return cuda_fail((cudaError_t)kr, "scatter kernel");
-  if (ev && ev[5]) cudaEventRecord(ev[5], s);
+  mark(8);
   kr = launch_raster(dviews, tile, sc, num_sms * tu.ctas_per_sm, tu.warps_per_cta, s);
   if (kr) return cuda_fail((cudaError_t)kr, "raster kernel");
-  if (ev) cudaEventRecord(ev[6], s);
+  mark(9);
   e = cudaMemcpyAsync(host + host_bytes, sc.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return cuda_fail(e, "read control block");
   return HSR_OK;
@@ -392,6 +401,9 @@ void Runtime::record_result(const Plan& p, const Ctl& c) {
   timing.h2d_bytes = p.host_bytes;
   timing.d2h_bytes = sizeof(Ctl);
   timing.views = (uint32_t)p.n;
+  timing.tiles = p.total_tiles;
+  timing.split_triangles = c.big_count;
+  timing.payload_bytes = c.pay_bytes;
 }
 
 int Runtime::run_batch(const hsr_draw_desc* descs, int n) {
@@ -406,9 +418,10 @@ int Runtime::run_batch(const hsr_draw_desc* descs, int n) {
     rc = staging.reserve(p.stage_bytes);
     if (rc != HSR_OK) return rc;
     p.bind(arena.base, staging.base);
-    cudaEvent_t evs[7] = {ev[0], profiling ? ev[1] : nullptr, profiling ? ev[2] : nullptr,
-                          profiling ? ev[3] : nullptr, profiling ? ev[4] : nullptr,
-                          profiling ? ev[5] : nullptr, ev[6]};
+    p.sc.faults = faults;
+    p.sc.poll_limit = poll_limit;
+    cudaEvent_t evs[kEvents];
+    for (int k = 0; k < kEvents; k++) evs[k] = (k == 0 || k == kEvents - 1 || profiling) ? ev[k] : nullptr;
     rc = p.enqueue(stream, num_sms, tuning, evs);
     if (rc != HSR_OK) return rc;
     launches += (uint64_t)p.kernel_count();
@@ -424,9 +437,9 @@ int Runtime::run_batch(const hsr_draw_desc* descs, int n) {
       return fail(HSR_ERR_TIMEOUT, "draw batch: a bounded device wait gave up");
     record_result(p, c);
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, ev[0], ev[6]);
+    cudaEventElapsedTime(&ms, ev[0], ev[kEvents - 1]);
     timing.batch_ms = ms;
-    for (int k = 0; k < 5; k++) {
+    for (int k = 0; k < HSR_KERNEL_COUNT; k++) {
       float km = 0.f;
       if (profiling) cudaEventElapsedTime(&km, ev[k + 1], ev[k + 2]);
       timing.kernel_ms[k] = km;
@@ -503,7 +516,7 @@ int hsr_init(int device) {
   }
   e = cudaStreamCreateWithFlags(&rt->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { delete rt; return cuda_fail(e, "cudaStreamCreate"); }
-  for (int k = 0; k < 7; k++) {
+  for (int k = 0; k < Runtime::kEvents; k++) {
     e = cudaEventCreate(&rt->ev[k]);
     if (e != cudaSuccess) { delete rt; return cuda_fail(e, "cudaEventCreate"); }
   }
@@ -521,7 +534,7 @@ int hsr_shutdown(void) {
   for (auto& kv : g_rt->targets) delete kv.second;
   if (g_rt->arena.base) cudaFree(g_rt->arena.base);
   if (g_rt->staging.base) cudaFreeHost(g_rt->staging.base);
-  for (int k = 0; k < 7; k++) cudaEventDestroy(g_rt->ev[k]);
+  for (int k = 0; k < Runtime::kEvents; k++) cudaEventDestroy(g_rt->ev[k]);
   cudaStreamDestroy(g_rt->stream);
   delete g_rt;
   g_rt = nullptr;
@@ -773,6 +786,16 @@ int hsr_set_tuning(const hsr_tuning* in) {
   if (in->ctas_per_sm < 1 || in->ctas_per_sm > 16) return fail(HSR_ERR_INVALID_ARG, "set_tuning: ctas_per_sm in [1,16]");
   if (!(in->bin_factor >= 0.5f && in->bin_factor <= 64.f)) return fail(HSR_ERR_INVALID_ARG, "set_tuning: bin_factor in [0.5,64]");
   g_rt->tuning = *in;
+  return HSR_OK;
+}
+
+int hsr_set_fault_injection(uint32_t faults, int32_t poll_limit) {
+  RT_OR_FAIL();
+  if (faults & ~(uint32_t)(HSR_FAULT_DEPENDENCY_STALL | HSR_FAULT_SCAN_STALL))
+    return fail(HSR_ERR_INVALID_ARG, "set_fault_injection: unknown fault bit");
+  if (poll_limit < 0) return fail(HSR_ERR_INVALID_ARG, "set_fault_injection: poll_limit must be >= 0");
+  g_rt->faults = faults;
+  g_rt->poll_limit = poll_limit;
   return HSR_OK;
 }
 

@@ -93,7 +93,10 @@ struct Runtime {
   uint64_t launches = 0;
   size_t cap_rec_hint = 0, cap_clip_hint = 0, cap_bin_hint = 0, cap_big_hint = 0;
   bool profiling = false;
-  cudaEvent_t ev[7] = {};
+  uint32_t faults = 0;     // hsr_set_fault_injection: HSR_FAULT_* for hsr_draw / hsr_draw_batch
+  int32_t poll_limit = 0;  // and the bounded waits' poll limit (0: default)
+  static constexpr int kEvents = HSR_KERNEL_COUNT + 2;  // start, after the memset, after each kernel
+  cudaEvent_t ev[kEvents] = {};
   hsr_timing timing = {};
 
   MeshObj* mesh(uint64_t h);

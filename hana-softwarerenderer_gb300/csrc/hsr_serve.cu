@@ -135,7 +135,11 @@ struct SrvReq {
   size_t bytes = 0;           // pool bytes of its targets
   char* mem = nullptr;        // one pool allocation: main planes then shadow planes
   uint64_t h_main = 0, h_shadow = 0;
+  int idle_alloc_failures = 0;  // failed allocations while no batch was in flight
 };
+// A request whose targets cannot be allocated while no batch is in flight (so no memory of
+// this server will free up) is failed after this many attempts.
+constexpr int kMaxIdleAllocFailures = 8;
 
 struct Slot {
   cudaStream_t stream = nullptr;  // copies of results, after the batch's kernels
@@ -166,6 +170,7 @@ struct ServerObj {
   uint64_t pool_used = 0;
   uint64_t next_ticket = 1;
   uint32_t next_batch = 1;
+  int inject_alloc_failures = 0;  // hsr_server_inject_alloc_failures (guarded by mu)
   bool stop = false;
   std::thread th;
   std::chrono::steady_clock::time_point t0;
@@ -306,16 +311,51 @@ static bool try_launch(ServerObj* so, Slot& s) {
     }
   }
   if (batch.empty()) return false;
+  // targets from the stream-ordered pool; from the first request whose allocation fails on,
+  // the requests go back to the head of the queue in arrival order (deferred, not failed)
+  size_t got = 0;
+  for (; got < batch.size(); got++) {
+    SrvReq* q = batch[got];
+    bool injected = false;
+    {
+      std::lock_guard<std::mutex> lk(so->mu);
+      if (so->inject_alloc_failures > 0) {
+        so->inject_alloc_failures--;
+        injected = true;
+      }
+    }
+    if (injected || cudaMallocAsync(reinterpret_cast<void**>(&q->mem), q->bytes, so->compute) != cudaSuccess) {
+      if (!injected) cudaGetLastError();
+      q->mem = nullptr;
+      break;
+    }
+  }
+  if (got < batch.size()) {
+    bool any_busy = false;
+    for (const Slot& o : so->slots) any_busy |= o.busy;
+    std::lock_guard<std::mutex> lk(so->mu);
+    for (size_t k = batch.size(); k-- > got;) {
+      SrvReq* q = batch[k];
+      so->pool_used -= q->bytes;
+      q->st.deferred++;
+      so->pending.push_front(q);
+    }
+    batch.resize(got);
+    if (batch.empty()) {
+      SrvReq* head = so->pending.front();
+      if (!any_busy && ++head->idle_alloc_failures >= kMaxIdleAllocFailures) {
+        so->pending.pop_front();
+        head->st.status = HSR_ERR_OUT_OF_MEMORY;
+        head->st.done_ms = so->now();
+        so->cv_done.notify_all();
+        return true;
+      }
+      return false;  // retried when a batch completes or after the scheduler's poll interval
+    }
+  }
   s.reqs = batch;
   s.batch = so->next_batch++;
   const double t = so->now();
-  // targets from the stream-ordered pool
-  for (SrvReq* q : batch) {
-    if (cudaMallocAsync(reinterpret_cast<void**>(&q->mem), q->bytes, so->compute) != cudaSuccess) {
-      cudaGetLastError();
-      q->mem = nullptr;
-    }
-  }
   s.descs.clear();
   int rc = HSR_OK;
   {
@@ -597,6 +637,15 @@ int hsr_server_wait(hsr_server s, uint64_t ticket, int32_t timeout_ms, hsr_reque
                                        [&] { return q->st.status != HSR_ERR_BUSY; });
   if (out) *out = q->st;
   if (!ok) return fail(HSR_ERR_TIMEOUT, "server_wait: timed out");
+  return HSR_OK;
+}
+
+int hsr_server_inject_alloc_failures(hsr_server s, int32_t n) {
+  ServerObj* so = server_of(s);
+  if (!so) return fail(HSR_ERR_BAD_HANDLE, "server_inject_alloc_failures: unknown server");
+  if (n < 0) return fail(HSR_ERR_INVALID_ARG, "server_inject_alloc_failures: n must be >= 0");
+  std::lock_guard<std::mutex> lk(so->mu);
+  so->inject_alloc_failures = n;
   return HSR_OK;
 }
 

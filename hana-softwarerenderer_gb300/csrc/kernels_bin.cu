@@ -20,7 +20,6 @@ constexpr int kScanTile = kScanThreads * kScanItems;  // tiles per scan block
 constexpr unsigned long long kFlagAgg = 1ull << 62;
 constexpr unsigned long long kFlagPre = 2ull << 62;
 constexpr unsigned long long kValMask = (1ull << 62) - 1;
-constexpr long kSpinLimit = 1L << 22;
 
 __host__ __device__ __forceinline__ int scan_blocks_hd(int ntiles) { return (ntiles + kScanTile - 1) / kScanTile; }
 int scan_blocks(int ntiles) { return scan_blocks_hd(ntiles); }
@@ -80,7 +79,18 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Scratch sc) {
       const unsigned long long agg = wi;
       unsigned long long* st = sc.scan_status;
       unsigned long long prefix = 0;
-      if (blk == 0) {
+      const long limit = sc.poll_limit > 0 ? (long)sc.poll_limit : kScanWaitPolls;
+      if (blk == 0 && (sc.faults & HSR_FAULT_SCAN_STALL)) {
+        // injected stall: withhold the prefix and wait on a word nothing sets (its own)
+        long spins = 0;
+        while ((ld_volatile64(&st[0]) >> 62) == 0) {
+          if (++spins > limit) {
+            atomicOr(&sc.ctl->error, kErrScanTimeout);
+            break;
+          }
+          __nanosleep(64);
+        }
+      } else if (blk == 0) {
         atomicExch(&st[0], kFlagPre | agg);
       } else {
         atomicExch(&st[blk], kFlagAgg | agg);
@@ -90,7 +100,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Scratch sc) {
         while (p >= 0) {
           const unsigned long long s = ld_volatile64(&st[p]);
           if ((s >> 62) == 0) {
-            if (++spins > kSpinLimit) {
+            if (++spins > limit) {
               atomicOr(&sc.ctl->error, kErrScanTimeout);
               break;
             }
@@ -145,7 +155,7 @@ __device__ __forceinline__ void scatter_records(const DView* __restrict__ views,
                                                 uint32_t nblocks) {
   const int lane = threadIdx.x & 31;
   const uint32_t nrec = min(sc.ctl->rec_count, sc.rec_cap);
-  if (sc.ctl->error & (kErrBinOverflow | kErrRecOverflow | kErrClipOverflow | kErrScanTimeout)) return;
+  if (sc.ctl->error & kErrNoDraw) return;
   const uint32_t stride = nblocks * blockDim.x;
   const int ts = __ffs(T) - 1;  // T is a power of two
   // warp-uniform trip count so every lane takes part in the warp-level collectives
@@ -193,7 +203,7 @@ __device__ __forceinline__ void scatter_records(const DView* __restrict__ views,
 // views' chunk bases when the batch has at most kSharedViews views (else null).
 __device__ __forceinline__ void clear_empty_tiles(const DView* __restrict__ views, int T, int nchunks, const Scratch& sc,
                                                   int block, int nblocks, const int32_t* cbase) {
-  if (sc.ctl->error & kErrCapacity) return;  // an overflowing sequence draws nothing
+  if (sc.ctl->error & kErrNoDraw) return;  // an overflowing or stalled sequence draws nothing
   const int ts = __ffs(T) - 1;
   const int nv = sc.nviews;
   const int lane = (int)threadIdx.x & 31, wpb = (int)blockDim.x >> 5;

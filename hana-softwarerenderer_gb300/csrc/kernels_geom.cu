@@ -552,6 +552,7 @@ __global__ void __launch_bounds__(kSetupThreads, 4) k_emit(const DView* __restri
   if (sc.ctl->error & kErrCapacity) return;
   const uint32_t nrec = min(sc.ctl->rec_count, sc.rec_cap);
   const uint32_t stride = gridDim.x * blockDim.x;
+  uint32_t pay_bytes = 0;  // payload bytes this lane wrote for the raster (big ones: k_big)
   for (uint32_t i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < nrec; i0 += stride) {
     const uint32_t i = i0 + (uint32_t)lane;
     bool valid = false;
@@ -576,7 +577,10 @@ __global__ void __launch_bounds__(kSetupThreads, 4) k_emit(const DView* __restri
     if (valid) rec_tiles(r, T, tx0, ty0, ntw, nt);
     const bool big = valid && nt > kMaxRecordTiles;
     const bool small = valid && !big;
-    if (small) r.pad = i;  // payload index
+    if (small) {
+      r.pad = i;  // payload index
+      pay_bytes += 16u * (uint32_t)nf4;
+    }
     append_counts(small, i, r, pl, nf4, *v, T, sc, true);
     const uint32_t bslot = warp_reserve(big, &sc.ctl->big_count);
     if (big) {
@@ -590,6 +594,8 @@ __global__ void __launch_bounds__(kSetupThreads, 4) k_emit(const DView* __restri
       }
     }
   }
+  pay_bytes = __reduce_add_sync(kFull, pay_bytes);
+  if (lane == 0 && pay_bytes) atomicAdd(&sc.ctl->pay_bytes, (unsigned long long)pay_bytes);
 }
 
 int launch_emit(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s) {
@@ -661,6 +667,8 @@ __device__ void clip_face(const DView& v, int view, int face, int T, const Scrat
   const int nf4 = payload_f4(v.shader);
   const uint32_t slot = warp_reserve(valid && !big, &sc.ctl->rec_count);
   append_small(valid && !big, slot, r, pl, nf4, v, T, sc);
+  const uint32_t pb = __reduce_add_sync(kFull, (valid && !big && slot < sc.rec_cap) ? 16u * (uint32_t)nf4 : 0u);
+  if (lane == 0 && pb) atomicAdd(&sc.ctl->pay_bytes, (unsigned long long)pb);
   const uint32_t bslot = warp_reserve(big, &sc.ctl->big_count);
   if (big) {
     if (bslot < sc.big_cap) {
@@ -736,6 +744,7 @@ __global__ void __launch_bounds__(kBigThreads) k_big(const DView* __restrict__ v
     const int nf4 = payload_f4(v.shader);
     if ((int)threadIdx.x < nf4)
       reinterpret_cast<float4*>(&sc.pay[base])[threadIdx.x] = reinterpret_cast<const float4*>(&bi.pay)[threadIdx.x];
+    if (threadIdx.x == 0 && nf4) atomicAdd(&sc.ctl->pay_bytes, 16ull * (unsigned long long)nf4);
     const int x0 = (int)(b.xr & 0xffffu), x1 = (int)(b.xr >> 16);
     const int y0 = (int)(b.yr & 0xffffu), y1 = (int)(b.yr >> 16);
     for (int sidx = threadIdx.x; sidx < nsub; sidx += kBigThreads) {

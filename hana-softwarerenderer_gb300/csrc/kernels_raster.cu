@@ -27,7 +27,6 @@
 namespace hsr {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr long kWaitLimit = 1L << 23;  // ~1-2 s of polling before a dependency wait gives up
 constexpr uint32_t kNone = 0xffffffffu;
 
 // View owning tile t: the last view whose first tile is <= t (views hold consecutive tile
@@ -43,14 +42,19 @@ __device__ __forceinline__ int find_view(const DView* views, const int32_t* tbas
 }
 
 // Wait until every non-empty tile of view `dep` is done (its empty tiles were cleared in the
-// scatter grid, which runs before the raster).
+// scatter grid, which runs before the raster).  Bounded: after the poll limit the wait sets
+// kErrWaitTimeout and returns, and once any wait of the sequence has given up the others
+// stop waiting (so a dependency that never completes costs one limit, not one per tile).
+// HSR_FAULT_DEPENDENCY_STALL makes the wait ask for one tile more than the view has.
 __device__ __forceinline__ void wait_view(const Scratch& sc, const DView* views, int dep) {
   if (dep < 0) return;
   const int tb = views[dep].tile_base;
-  const uint32_t need = sc.ne_off[tb + views[dep].ntiles] - sc.ne_off[tb];
+  const uint32_t need = sc.ne_off[tb + views[dep].ntiles] - sc.ne_off[tb] +
+                        ((sc.faults & HSR_FAULT_DEPENDENCY_STALL) ? 1u : 0u);
+  const long limit = sc.poll_limit > 0 ? (long)sc.poll_limit : kDepWaitPolls;
   long spins = 0;
   while (*reinterpret_cast<volatile uint32_t*>(&sc.view_done[dep]) < need) {
-    if (++spins > kWaitLimit) {
+    if (++spins > limit || (*reinterpret_cast<volatile uint32_t*>(&sc.ctl->error) & kErrWaitTimeout)) {
       atomicOr(&sc.ctl->error, kErrWaitTimeout);
       return;
     }
@@ -214,7 +218,7 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
     const uint32_t gw = blockIdx.x * (uint32_t)WARPS + (uint32_t)warp;
     if (sc.stash && gw < sc.stash_warps) stash = sc.stash + (size_t)gw * kStashFloats;
   }
-  if (sc.ctl->error & kErrCapacity) return;
+  if (sc.ctl->error & kErrNoDraw) return;
   const uint32_t nrec = min(sc.ctl->rec_count, sc.rec_cap);
 
   // The non-empty tiles are handed out by one counter over their list, two ahead: while a

@@ -46,16 +46,18 @@ class Tuning(ctypes.Structure):
                 ("bin_factor", ctypes.c_float)]
 
 
+# kernels of one launch sequence, in launch order (hsr_timing.kernel_ms)
+KERNELS = ("vertex", "cull", "emit", "clip", "split", "scan", "scatter", "raster")
+
+
 class Timing(ctypes.Structure):
-    _fields_ = [("batch_ms", ctypes.c_float), ("kernel_ms", ctypes.c_float * 5), ("launches", ctypes.c_uint32),
-                ("views", ctypes.c_uint32), ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
-                ("pixels", ctypes.c_uint64), ("shaded_pixels", ctypes.c_uint64), ("records", ctypes.c_uint64),
-                ("bin_pairs", ctypes.c_uint64), ("faces", ctypes.c_uint64), ("vertices", ctypes.c_uint64),
-                ("normals", ctypes.c_uint64), ("clipped_faces", ctypes.c_uint64), ("fragments", ctypes.c_uint64),
-                ("raster_pixels", ctypes.c_uint64)]
-
-
-KERNELS = ("vertex", "setup", "scan", "scatter", "raster")
+    _fields_ = [("batch_ms", ctypes.c_float), ("kernel_ms", ctypes.c_float * len(KERNELS)),
+                ("launches", ctypes.c_uint32), ("views", ctypes.c_uint32), ("h2d_bytes", ctypes.c_uint64),
+                ("d2h_bytes", ctypes.c_uint64), ("pixels", ctypes.c_uint64), ("shaded_pixels", ctypes.c_uint64),
+                ("records", ctypes.c_uint64), ("bin_pairs", ctypes.c_uint64), ("faces", ctypes.c_uint64),
+                ("vertices", ctypes.c_uint64), ("normals", ctypes.c_uint64), ("clipped_faces", ctypes.c_uint64),
+                ("fragments", ctypes.c_uint64), ("raster_pixels", ctypes.c_uint64), ("tiles", ctypes.c_uint64),
+                ("split_triangles", ctypes.c_uint64), ("payload_bytes", ctypes.c_uint64)]
 
 
 class Stats(ctypes.Structure):
@@ -93,7 +95,7 @@ class SceneParams(ctypes.Structure):
 
 class RequestStatus(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int32), ("batch", ctypes.c_uint32), ("batch_requests", ctypes.c_uint32),
-                ("pad", ctypes.c_uint32), ("submit_ms", ctypes.c_double), ("launch_ms", ctypes.c_double),
+                ("deferred", ctypes.c_uint32), ("submit_ms", ctypes.c_double), ("launch_ms", ctypes.c_double),
                 ("done_ms", ctypes.c_double)]
 
 
@@ -153,6 +155,8 @@ def lib():
                             ctypes.c_int),
         "hsr_server_now_ms": ([ctypes.c_uint64, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
         "hsr_server_destroy": ([ctypes.c_uint64], ctypes.c_int),
+        "hsr_server_inject_alloc_failures": ([ctypes.c_uint64, ctypes.c_int32], ctypes.c_int),
+        "hsr_set_fault_injection": ([ctypes.c_uint32, ctypes.c_int32], ctypes.c_int),
         "hsr_shader_data_build": ([ctypes.POINTER(SceneParams), ctypes.c_void_p], ctypes.c_int),
         "hsr_model_matrix": ([ctypes.POINTER(Transform), _f32p], ctypes.c_int),
         "hsr_matrix_invert": ([_f32p, _f32p], ctypes.c_int),
@@ -223,6 +227,16 @@ def stats() -> dict:
     s = Stats()
     check(lib().hsr_get_stats(ctypes.byref(s)))
     return {k: int(getattr(s, k)) for k, _ in Stats._fields_}
+
+
+FAULT_DEPENDENCY_STALL = 1
+FAULT_SCAN_STALL = 2
+
+
+def set_fault_injection(faults: int = 0, poll_limit: int = 0) -> None:
+    """hsr_set_fault_injection: make a bounded device wait of hsr_draw / hsr_draw_batch run out
+    (FAULT_* mask) after `poll_limit` polls (0: the default limit)."""
+    check(lib().hsr_set_fault_injection(faults, poll_limit))
 
 
 def set_profiling(on: bool) -> None:
@@ -588,7 +602,11 @@ class Server:
 
     @staticmethod
     def _status(st: RequestStatus) -> dict:
-        return {k: getattr(st, k) for k, _ in RequestStatus._fields_ if k != "pad"}
+        return {k: getattr(st, k) for k, _ in RequestStatus._fields_}
+
+    def inject_alloc_failures(self, n: int) -> None:
+        """The next n target allocations fail as if the memory pool were exhausted."""
+        check(lib().hsr_server_inject_alloc_failures(self.handle, n))
 
     def poll(self, ticket: int) -> dict | None:
         st = RequestStatus()

@@ -212,8 +212,17 @@ def serve_batched(rp: ResidentPool, reqs: list, pool_bytes: int = 40 << 30, max_
             reclaim_one()
         wall = time.perf_counter() - t0
     finally:
+        # results still in flight are copied into the ring: wait for them before its memory
+        # goes (a server we own finishes its batches when closed; one passed in keeps running)
         if own:
             srv.close()
+        else:
+            while outstanding:
+                i, tk = outstanding.popleft()
+                try:
+                    srv.wait(tk)
+                except Exception:  # noqa: BLE001  the original error is the one to raise
+                    pass
         if own_ring:
             ring.release()
     lat = np.array([status[i]["done_ms"] - (srv_t0 + reqs[i].arrival_ms) for i in range(len(reqs))])

@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define HSR_ABI_VERSION 1
+#define HSR_ABI_VERSION 2
 
 /* ---- status codes ---------------------------------------------------------------- */
 enum {
@@ -225,18 +225,23 @@ HSR_API int hsr_draw(const hsr_draw_desc* desc);
 HSR_API int hsr_draw_batch(const hsr_draw_desc* descs, int32_t n);
 HSR_API int hsr_synchronize(void);
 
-/* hsr_draw_noalloc: the same draw as hsr_draw, for callers that must not allocate while
- * drawing — work recorded into a CUDA graph (allocation is not allowed during stream
- * capture), real-time loops that cannot stall on cudaMalloc's device-wide
- * synchronisation, and processes held to a fixed device-memory budget.  It has no
- * counterpart in the reference.  Meshes, textures and targets are the caller's existing
- * handles; the call's own scratch is one fixed 128 MiB device array that every GPU loading
- * this library holds until exit, so it calls no cudaMalloc, cudaFree or cudaMallocHost.
- * A draw needing more than 128 MiB of scratch is refused with HSR_ERR_INVALID_ARG (roughly
- * 400k faces into 1920x1080); one that overflows the fixed split on the device returns
- * HSR_ERR_BIN_OVERFLOW with the target untouched.  All calls share the array: calls whose
- * GPU work overlaps race, so issue them one after another.  The first call on a device
- * looks up the array's address on that device; make it before any stream capture. */
+/* hsr_draw_noalloc: the same draw as hsr_draw, for callers that must not allocate device or
+ * page-locked host memory while they draw.  It has no counterpart in the reference.  Such
+ * callers are render loops with a frame deadline (cudaMalloc and cudaFree can synchronise
+ * the whole device and stall the loop for milliseconds), processes held to a fixed
+ * device-memory budget that may not grow after start-up (a GPU shared with other services,
+ * where a growing allocation can fail in the middle of a frame), and host applications that
+ * forbid allocation inside their per-frame callbacks.  Meshes, textures and targets are the
+ * caller's existing handles; the draw's own scratch is one fixed 128 MiB device array inside
+ * the library, which every GPU that loads the library holds until the process exits, so the
+ * call makes no cudaMalloc, cudaFree, cudaMallocHost or other allocating call.  A draw needing
+ * more than 128 MiB of scratch is refused with HSR_ERR_INVALID_ARG (roughly 400k faces into
+ * 1920x1080); one that overflows the fixed split on the device returns HSR_ERR_BIN_OVERFLOW
+ * with the target untouched.  The call runs on the library's stream and returns when the
+ * draw is complete.  Every call shares the array and it keeps the previous call's contents
+ * (each call clears the counters it needs): calls whose GPU work overlaps race, so issue
+ * them one after another.  The first call on a device looks up the array's address on that
+ * device (cudaGetSymbolAddress); make that first call before any stream capture begins. */
 HSR_API int hsr_draw_noalloc(const hsr_draw_desc* desc);
 
 /* ---- tuning ------------------------------------------------------------------------- */
@@ -252,6 +257,22 @@ HSR_API int hsr_set_tuning(const hsr_tuning* in);
  * renders it `reps` times into its targets), set them, size the bin capacity from the
  * observed (triangle, tile) pairs, and return the choice in `out` (may be NULL). */
 HSR_API int hsr_autotune(const hsr_draw_desc* descs, int32_t n, int32_t reps, hsr_tuning* out);
+
+/* ---- failure injection for tests of the bounded device waits --------------------------
+ * Host-side switches for hsr_draw / hsr_draw_batch (not plans or servers); no GPU fault is
+ * involved.  poll_limit is the number of polls after which a bounded device wait gives up
+ * (0 restores the default, about one second); once one dependency wait of a launch sequence
+ * has given up, the others of that sequence stop waiting too.  faults is a mask of:
+ *   HSR_FAULT_DEPENDENCY_STALL  raster tiles of a draw that reads another draw's target (its
+ *                               shadow map) wait for one finished tile more than that draw
+ *                               has, so the wait ends only by running out: the call returns
+ *                               HSR_ERR_TIMEOUT and the device stays usable;
+ *   HSR_FAULT_SCAN_STALL        the tile-count scan's first block withholds its prefix and
+ *                               waits for a flag nothing sets, so every look-back runs out:
+ *                               the call returns HSR_ERR_TIMEOUT and writes no target. */
+#define HSR_FAULT_DEPENDENCY_STALL 1u
+#define HSR_FAULT_SCAN_STALL 2u
+HSR_API int hsr_set_fault_injection(uint32_t faults, int32_t poll_limit);
 
 /* ---- statistics of the last completed draw sequence (for tests and benchmarks) ------- */
 typedef struct hsr_stats {
@@ -318,7 +339,9 @@ typedef struct hsr_request_status {
   int32_t status;          /* HSR_OK, HSR_ERR_BUSY while pending, or the failure        */
   uint32_t batch;          /* sequence number of the batch that rendered it             */
   uint32_t batch_requests; /* requests in that batch                                    */
-  uint32_t pad;
+  uint32_t deferred;       /* times its targets could not be allocated at admission: the
+                              request then stays queued at its place in arrival order and
+                              is admitted again once memory frees up                    */
   double submit_ms;        /* times on the server's clock (ms since creation)           */
   double launch_ms;
   double done_ms;
@@ -330,14 +353,29 @@ HSR_API int hsr_server_poll(hsr_server s, uint64_t ticket, hsr_request_status* o
 HSR_API int hsr_server_wait(hsr_server s, uint64_t ticket, int32_t timeout_ms, hsr_request_status* out);
 HSR_API int hsr_server_now_ms(hsr_server s, double* out);
 HSR_API int hsr_server_destroy(hsr_server s);   /* finishes in-flight work, fails queued requests */
+/* Failure injection for tests of the admission path: the next n target allocations of the
+ * server fail as if the device's memory pool were exhausted (no allocation is attempted).
+ * Requests whose allocation fails are deferred, not failed: they stay queued in arrival
+ * order and are admitted again when memory frees up; a request that still cannot get memory
+ * with no batch in flight is failed with HSR_ERR_OUT_OF_MEMORY after 8 attempts. */
+HSR_API int hsr_server_inject_alloc_failures(hsr_server s, int32_t n);
 
 /* ---- timing of the last completed draw sequence (CUDA events on the library stream) --
  * batch_ms spans the upload of the view descriptors to the end of the raster kernel;
- * kernel_ms = {vertex, setup + post (clip / split), scan, scatter, raster}, filled when
- * profiling is on. */
+ * kernel_ms holds one entry per kernel of the launch sequence, in launch order, filled when
+ * profiling is on:
+ *   [0] vertex   screen vertices (k_vertex)
+ *   [1] cull     fast accept, cull, viewport, bounding box, record (k_setup)
+ *   [2] emit     shading payloads and tile counts of the surviving triangles (k_emit)
+ *   [3] clip     homogeneous clipper for faces crossing a plane (k_post)
+ *   [4] split    sub-records of triangles touching many tiles (k_big)
+ *   [5] scan     prefix sums over the tile counts (k_scan)
+ *   [6] scatter  tile lists, and the clear of tiles without triangles (k_scatter)
+ *   [7] raster   coverage, depth test, shading, writes (k_raster) */
+#define HSR_KERNEL_COUNT 8
 typedef struct hsr_timing {
   float batch_ms;
-  float kernel_ms[5];
+  float kernel_ms[HSR_KERNEL_COUNT];
   uint32_t launches;       /* kernels launched by the sequence                         */
   uint32_t views;          /* draws in the sequence                                    */
   uint64_t h2d_bytes;      /* host -> device bytes of the sequence (view descriptors)  */
@@ -354,6 +392,9 @@ typedef struct hsr_timing {
   uint64_t fragments;      /* covered (pixel, triangle) pairs tested against the depth  */
   uint64_t raster_pixels;  /* pixels of the tiles the raster visited (tiles with triangles;
                               the fused clear of the others runs beside the binning)    */
+  uint64_t tiles;          /* screen tiles of the sequence (all views)                  */
+  uint64_t split_triangles;/* triangles split into sub-records (more than 32 tiles)     */
+  uint64_t payload_bytes;  /* shading payload bytes written for the raster's records    */
 } hsr_timing;
 HSR_API int hsr_set_profiling(int on);
 HSR_API int hsr_last_timing(hsr_timing* out);

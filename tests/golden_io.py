@@ -43,3 +43,20 @@ def compare(got: dict, exp: dict, color_tol: int = 1) -> dict:
     return {"depth_mismatch": d_bad, "prim_mismatch": p_bad, "color_max_err": int(dc.max()) if dc.size else 0,
             "color_diff_px": int((dc.max(axis=-1) > 0).sum()), "alpha_mismatch": a_bad,
             "color_ok": bool(dc.max() <= color_tol) if dc.size else True}
+
+
+def assert_pass(got: dict, exp: dict, pass_name: str, label: str = "", color_tol: int = 1) -> dict:
+    """Parity of one pass against the reference (or the oracle): depth, prim ids and alpha bit
+    for bit; RGB within `color_tol` LSB for the main pass (BlinnShader / NormalMapShader call
+    powf, which is not correctly rounded), and bit for bit for the shadow pass (ShadowShader,
+    IShader.cpp:176-180, has no powf).  Prints and returns the report: max colour error and the
+    count of differing pixels."""
+    rep = compare(got, exp, color_tol)
+    print(label, pass_name, rep)
+    assert rep["depth_mismatch"] == 0, (label, pass_name, rep)
+    assert rep["prim_mismatch"] == 0, (label, pass_name, rep)
+    assert rep["alpha_mismatch"] == 0, (label, pass_name, rep)
+    assert rep["color_ok"], (label, pass_name, rep)
+    if pass_name == "shadow":
+        assert rep["color_diff_px"] == 0, (label, pass_name, rep)
+    return rep

@@ -43,7 +43,7 @@ def test_no_device_means_error_not_fallback(libpath):
     import hsr
 
     L = hsr.lib()
-    assert L.hsr_abi_version() == 1
+    assert L.hsr_abi_version() == 2
     rc = L.hsr_init(0)
     assert rc == hsr.ERR_CUDA
     assert b"device" in L.hsr_last_error() or len(L.hsr_last_error()) > 0
@@ -63,9 +63,10 @@ def test_struct_layouts_match_header(tmp_path):
     checks = {
         "hsr_draw_desc": (hsr.DrawDesc, ["uniforms", "prim_base", "clear_rgba"]),
         "hsr_request": (hsr.Request, ["uniforms", "clear_rgba", "shadow_clear_depth", "out_rgba", "out_prim"]),
-        "hsr_request_status": (hsr.RequestStatus, ["submit_ms", "done_ms"]),
+        "hsr_request_status": (hsr.RequestStatus, ["deferred", "submit_ms", "done_ms"]),
         "hsr_server_config": (hsr.ServerConfig, ["max_batch", "slots"]),
-        "hsr_timing": (hsr.Timing, ["launches", "h2d_bytes", "clipped_faces", "fragments", "raster_pixels"]),
+        "hsr_timing": (hsr.Timing, ["launches", "h2d_bytes", "clipped_faces", "fragments", "raster_pixels", "tiles",
+                                     "payload_bytes"]),
         "hsr_stats": (hsr.Stats, ["kernel_launches"]),
         "hsr_tuning": (hsr.Tuning, ["bin_factor"]),
         "hsr_transform": (hsr.Transform, ["rotation", "scale"]),

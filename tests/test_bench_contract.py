@@ -15,20 +15,27 @@ sys.path.insert(0, ROOT)
 import bench  # noqa: E402
 
 COUNTS = {"faces": 50_884_881, "vertices": 25_466_468, "normals": 0, "records": 9_128_663, "bin_pairs": 13_002_767,
-          "pixels": 133_068_066, "shaded_pixels": 51_022_263, "clipped_faces": 84_957, "raster_pixels": 52_734_190}
+          "pixels": 133_068_066, "shaded_pixels": 51_022_263, "clipped_faces": 84_957, "raster_pixels": 52_734_190,
+          "tiles": 1_842_000, "split_triangles": 1_200, "payload_bytes": 9_128_663 * 96}
 
 
-def test_roofline_reports_the_largest_single_kernel():
-    """The setup segment holds four kernels; the roofline names the largest one-kernel segment,
-    and frac = achieved / peak with achieved = algorithmic bytes / the segment's time."""
-    km = {"vertex": [0.12], "setup": [2.2], "scan": [0.02], "scatter": [0.39], "raster": [2.1]}
+def test_roofline_reports_every_kernel_and_the_largest():
+    """Every kernel of the launch sequence gets its share, algorithmic bytes and fraction of
+    the peak; the headline is the kernel with the largest share, frac = achieved / peak with
+    achieved = algorithmic bytes / the kernel's time."""
+    km = {"vertex": [0.12], "cull": [0.87], "emit": [0.51], "clip": [0.2], "split": [0.05], "scan": [0.02],
+          "scatter": [0.39], "raster": [2.1]}
     r = bench.roofline(km, COUNTS, "serve_batch64")
     assert r["kernel"] == "raster"
-    kb = bench.kernel_bytes(COUNTS)["raster"]
-    assert r["algorithmic_bytes"] == int(kb)
-    assert abs(r["achieved"] - kb / 2.1e-3 / 1e9) < 0.1
+    kb = bench.kernel_bytes(COUNTS)
+    assert r["algorithmic_bytes"] == int(kb["raster"])
+    assert abs(r["achieved"] - kb["raster"] / 2.1e-3 / 1e9) < 0.1
     assert abs(r["frac"] - r["achieved"] / r["peak"]) < 1e-3
-    assert abs(sum(r["share"].values()) - 1.0) < 1e-3
+    assert set(r["kernels"]) == set(km)
+    assert abs(sum(k["share"] for k in r["kernels"].values()) - 1.0) < 1e-3
+    for name, k in r["kernels"].items():
+        assert k["algorithmic_bytes"] == int(kb[name])
+        assert abs(k["frac"] - k["achieved_gbs"] / r["peak"]) < 1e-3
 
 
 def test_clear_bytes_move_from_raster_to_scatter():

@@ -70,9 +70,7 @@ def expect(frame):
 
 def check(got, exp, label):
     for k in exp:
-        rep = golden_io.compare(got[k], exp[k], 1)
-        assert rep["depth_mismatch"] == 0 and rep["prim_mismatch"] == 0 and rep["alpha_mismatch"] == 0, (label, k, rep)
-        assert rep["color_ok"], (label, k, rep)
+        golden_io.assert_pass(got[k], exp[k], k, label)
 
 
 @pytest.mark.parametrize("seed", range(48))

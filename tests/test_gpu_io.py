@@ -71,10 +71,7 @@ def test_loaded_obj_and_tga_render_like_the_oracle(gpu, tmp_path):
     exp = {"main": {"depth": mb.depth, "color": mb.color, "prim": mb.prim},
            "shadow": {"depth": sm.depth, "color": sm.color, "prim": sm.prim}}
     for k in exp:
-        rep = golden_io.compare(got[k], exp[k], 1)
-        print("loaded assets", k, rep)
-        assert rep["depth_mismatch"] == 0 and rep["prim_mismatch"] == 0 and rep["alpha_mismatch"] == 0, rep
-        assert rep["color_ok"], rep
+        golden_io.assert_pass(got[k], exp[k], k, "loaded assets")
     # the normals matter: drawn with the stored normals the image differs
     assert (got["main"]["prim"] > 0).sum() > 1000
 

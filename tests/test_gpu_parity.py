@@ -30,12 +30,7 @@ def gpu_render(gpu, frame, batched=True):
 
 def assert_parity(got, exp, label):
     for k, e in exp.items():
-        rep = golden_io.compare(got[k], e, COLOR_TOL)
-        print(label, k, rep)
-        assert rep["depth_mismatch"] == 0, (label, k, rep)
-        assert rep["prim_mismatch"] == 0, (label, k, rep)
-        assert rep["alpha_mismatch"] == 0, (label, k, rep)
-        assert rep["color_ok"], (label, k, rep)
+        golden_io.assert_pass(got[k], e, k, label, COLOR_TOL)
 
 
 def oracle_expect(frame):

@@ -16,11 +16,7 @@ def test_oracle_matches_reference(name):
     out = oracle.render_frame(frame)
     for k, e in exp.items():
         got = {"depth": out[k].depth, "color": out[k].color, "prim": out[k].prim}
-        rep = golden_io.compare(got, e)
-        assert rep["depth_mismatch"] == 0, (k, rep)
-        assert rep["prim_mismatch"] == 0, (k, rep)
-        assert rep["alpha_mismatch"] == 0, (k, rep)
-        assert rep["color_ok"], (k, rep)
+        golden_io.assert_pass(got, e, k, name)
 
 
 def test_oracle_built_without_contraction():

@@ -173,10 +173,8 @@ def test_server_vs_oracle(gpu, rp):
     tex = scenes.pool_textures(2, 256, seed=5)
     for r, o in zip(reqs, outs):
         exp = oracle.render_frame(scenes.view_frame(r, rp.pool, tex))["main"]
-        rep = golden_io.compare(o, {"color": exp.color, "depth": exp.depth, "prim": exp.prim}, 1)
-        print(r.width, r.height, scenes.SHADER_NAMES[r.shader], r.shadow, rep)
-        assert rep["depth_mismatch"] == 0 and rep["prim_mismatch"] == 0 and rep["alpha_mismatch"] == 0, rep
-        assert rep["color_ok"], rep
+        golden_io.assert_pass(o, {"color": exp.color, "depth": exp.depth, "prim": exp.prim}, "main",
+                              f"{r.width}x{r.height} {scenes.SHADER_NAMES[r.shader]} shadow {r.shadow}")
 
 
 def test_server_admission_by_memory(gpu, rp):

@@ -1,16 +1,21 @@
-"""GPU: hsr_draw_noalloc, the draw entry point for callers that cannot allocate while they
-draw (work captured into a CUDA graph, real-time loops, fixed memory budgets).
+"""GPU: hsr_draw_noalloc, the draw entry point for callers that must not allocate while they
+draw: render loops with a frame deadline (cudaMalloc / cudaFree can synchronise the whole
+device), processes held to a fixed device-memory budget, and hosts that forbid allocation in
+their per-frame callbacks.
 
 It must produce what hsr_draw produces — depth and prim ids bit for bit, colour within the
 1 LSB the parity tests allow — on two calls in a row, since every call reuses the same
-fixed scratch array and must clear whatever has to start from zero.  This file is named to
-be collected last, and it initialises the library itself so it also passes alone in a
-fresh process.
+fixed scratch array and must clear whatever has to start from zero; one call is also checked
+against the oracle directly, and a draw that overflows the fixed split must leave its target
+untouched.  This file is named to be collected last, and it initialises the library itself
+so it also passes alone in a fresh process.
 """
 import numpy as np
 import pytest
 
+import golden_io
 import hsr
+import oracle
 from hsr import frame as hframe
 from hsr import scenes
 
@@ -58,3 +63,41 @@ def test_noalloc_draw_refuses_oversized_draws():
         assert e.value.code == hsr.ERR_INVALID_ARG
     finally:
         g.release()
+
+
+def test_noalloc_draw_matches_the_oracle():
+    hsr.init(0)
+    fr = scenes.displaced_frame(4, 256, 192, shadow=256, tex_size=64, seed=9)
+    g = hframe.GpuFrame(fr)
+    try:
+        for d in g.descs:
+            hsr.draw_noalloc(d)
+        got = g.download()
+    finally:
+        g.release()
+    exp = oracle.render_frame(fr)
+    for k, e in exp.items():
+        golden_io.assert_pass(got[k], {"depth": e.depth, "color": e.color, "prim": e.prim}, k, "noalloc")
+
+
+def test_noalloc_overflow_leaves_the_target_untouched():
+    """With the bin capacity at half a (triangle, tile) pair per triangle and tile, a soup of
+    triangles spanning several 8x8 tiles overflows the fixed split on the device: the call
+    returns HSR_ERR_BIN_OVERFLOW and the target keeps every byte it had."""
+    hsr.init(0)
+    old = hsr.get_tuning()
+    fr = scenes.soup_frame(20_000, 640, 480, seed=13, median_edge_px=6.0)
+    g = hframe.GpuFrame(fr)
+    try:
+        hsr.set_tuning(tile=8, warps_per_cta=4, bin_factor=0.5)
+        g.main.clear((9, 8, 7, 6), 0.25)
+        before = g.main.download()
+        with pytest.raises(hsr.HsrError) as e:
+            hsr.draw_noalloc(g.descs[0])
+        assert e.value.code == hsr.ERR_BIN_OVERFLOW
+        after = g.main.download()
+        for p in ("color", "depth", "prim"):
+            assert np.array_equal(before[p], after[p]), p
+    finally:
+        g.release()
+        hsr.set_tuning(tile=old.tile, warps_per_cta=old.warps_per_cta, bin_factor=old.bin_factor)
