@@ -189,14 +189,14 @@ struct Scratch {
   uint32_t* bins;   uint32_t bin_cap;
   int32_t ntiles;
   int32_t nviews;
-  float* stash;             // [stash_warps][kStashFloats] per raster warp (may be null)
+  float* stash;             // [stash_warps][stash_floats(tile)] per raster warp (may be null)
   uint32_t stash_warps;
   uint32_t faults;          // HSR_FAULT_* injected by the host (tests of the failure paths)
   int32_t poll_limit;       // polls before a bounded wait gives up (0: the defaults above)
 };
-// Per raster warp of a 16x16 tile: the winner's weights b0, b1, b2, payload index and
-// submission per pixel (what shading would otherwise re-derive from the record).
-constexpr int kStashFloats = 5 * 256;
+// Per raster warp of a 16x16 or 32x32 tile: the winner's weights b0, b1, b2, payload index
+// and submission per pixel (what shading would otherwise re-derive from the record).
+__host__ __device__ constexpr int stash_floats(int tile) { return 5 * tile * tile; }
 constexpr int kStashWarpsPerSm = 32;  // raster warps resident per SM at most
 
 // Kernel launchers (kernels_*.cu).  All return cudaError_t as int.

@@ -178,7 +178,7 @@ int Runtime::plan_build(const hsr_draw_desc* descs, int n, Plan& p) {
   p = Plan();
   p.n = n;
   p.tile = T;
-  p.stash_warps = T == 16 ? (uint32_t)num_sms * kStashWarpsPerSm : 0u;  // 8x8 tiles keep theirs in shared memory
+  p.stash_warps = T >= 16 ? (uint32_t)num_sms * kStashWarpsPerSm : 0u;  // 8x8 tiles keep theirs in shared memory
   p.views.resize(n);
   p.offs.resize(n);
   p.order = order;
@@ -280,7 +280,7 @@ void Plan::layout() {
   o_clip = off; off = align_up(off + sizeof(int2) * clip_cap, 256);
   o_big = off; off = align_up(off + sizeof(BigItem) * big_cap, 256);
   o_bins = off; off = align_up(off + sizeof(uint32_t) * bin_cap, 256);
-  o_stash = off; off = align_up(off + sizeof(float) * kStashFloats * (size_t)stash_warps, 256);
+  o_stash = off; off = align_up(off + sizeof(float) * (size_t)stash_floats(tile) * (size_t)stash_warps, 256);
   dev_bytes = off;
   stage_bytes = host_bytes + sizeof(Ctl);
 }
@@ -780,9 +780,11 @@ int hsr_get_tuning(hsr_tuning* out) {
 int hsr_set_tuning(const hsr_tuning* in) {
   RT_OR_FAIL();
   if (!in) return fail(HSR_ERR_INVALID_ARG, "set_tuning: null");
-  if (in->tile != 8 && in->tile != 16) return fail(HSR_ERR_INVALID_ARG, "set_tuning: tile must be 8 or 16");
+  if (in->tile != 8 && in->tile != 16 && in->tile != 32)
+    return fail(HSR_ERR_INVALID_ARG, "set_tuning: tile must be 8, 16 or 32");
   if (in->warps_per_cta != 4 && in->warps_per_cta != 8) return fail(HSR_ERR_INVALID_ARG, "set_tuning: warps_per_cta must be 4 or 8");
-  if (in->tile == 16 && in->warps_per_cta != 4) return fail(HSR_ERR_INVALID_ARG, "set_tuning: tile 16 runs 4 warps per CTA");
+  if (in->tile >= 16 && in->warps_per_cta != 4)
+    return fail(HSR_ERR_INVALID_ARG, "set_tuning: tiles of 16 and 32 run 4 warps per CTA");
   if (in->ctas_per_sm < 1 || in->ctas_per_sm > 16) return fail(HSR_ERR_INVALID_ARG, "set_tuning: ctas_per_sm in [1,16]");
   if (!(in->bin_factor >= 0.5f && in->bin_factor <= 64.f)) return fail(HSR_ERR_INVALID_ARG, "set_tuning: bin_factor in [0.5,64]");
   g_rt->tuning = *in;
@@ -829,25 +831,30 @@ int hsr_host_free(void* p) {
   return e == cudaSuccess ? HSR_OK : cuda_fail(e, "host_free");
 }
 
-// Autotuner: renders the batch with each candidate (tile 8/16, warps per CTA 4/8, CTAs per
-// SM 1..8), keeps the fastest median device time, and sizes the bin capacity from the
-// (triangle, tile) pairs it observed.  The batch's targets receive `reps` renders per
-// candidate.
+// Autotuner: renders the batch with each launch shape (tile 8 / 16 / 32, warps per CTA 4 / 8,
+// CTAs per SM 1..8), keeps the fastest median device time, then searches the bin capacity:
+// the smallest factor of a ladder with which the batch runs without a bin overflow (capacity
+// hints learnt from earlier overflows set aside during the search), plus a quarter of headroom
+// for the next batches of a stream.  The batch's targets receive the renders.
 int hsr_autotune(const hsr_draw_desc* descs, int32_t n, int32_t reps, hsr_tuning* out) {
   RT_OR_FAIL();
   if (!descs || n <= 0 || reps <= 0) return fail(HSR_ERR_INVALID_ARG, "autotune: bad arguments");
   const hsr_tuning saved = g_rt->tuning;
   const bool saved_prof = g_rt->profiling;
   g_rt->profiling = false;
+  auto restore = [&](int rc) {
+    g_rt->tuning = saved;
+    g_rt->profiling = saved_prof;
+    return rc;
+  };
   hsr_tuning best = saved;
   float best_ms = 1e30f;
-  double pairs_per_item = 0.0;
-  const int tiles[2] = {8, 16}, warps[2] = {4, 8}, ctas[4] = {1, 2, 4, 8};
+  const int tiles[3] = {8, 16, 32}, warps[2] = {4, 8}, ctas[4] = {1, 2, 4, 8};
   for (int ti : tiles)
     for (int wi : warps)
       for (int ci : ctas) {
-        if (ci * wi > 32) continue;  // beyond one SM's warp slots for these kernels
-        if (ti == 16 && wi != 4) continue;  // shared-memory budget of the 16x16 tile
+        if (ci * wi > 32) continue;          // beyond one SM's warp slots for these kernels
+        if (ti >= 16 && wi != 4) continue;   // shared-memory budget of the 16x16 and 32x32 tiles
         hsr_tuning cand = saved;
         cand.tile = ti;
         cand.warps_per_cta = wi;
@@ -856,11 +863,7 @@ int hsr_autotune(const hsr_draw_desc* descs, int32_t n, int32_t reps, hsr_tuning
         std::vector<float> ms;
         for (int r = 0; r < reps + 1; r++) {
           int rc = g_rt->run_batch(descs, n);
-          if (rc != HSR_OK) {
-            g_rt->tuning = saved;
-            g_rt->profiling = saved_prof;
-            return rc;
-          }
+          if (rc != HSR_OK) return restore(rc);
           if (r > 0) ms.push_back(g_rt->timing.batch_ms);  // first run warms up
         }
         std::sort(ms.begin(), ms.end());
@@ -869,10 +872,29 @@ int hsr_autotune(const hsr_draw_desc* descs, int32_t n, int32_t reps, hsr_tuning
           best_ms = med;
           best = cand;
         }
-        const double items = (double)g_rt->timing.faces + (double)g_rt->timing.pixels / (double)(ti * ti);
-        if (items > 0) pairs_per_item = std::max(pairs_per_item, (double)g_rt->timing.bin_pairs / items);
       }
-  best.bin_factor = (float)std::min(64.0, std::max(1.0, pairs_per_item * 1.25));
+  // bin capacity = factor * (faces + tiles) + 4096 pairs
+  const float ladder[] = {0.5f, 0.75f, 1.f, 1.5f, 2.f, 3.f, 4.f, 6.f, 8.f, 12.f, 16.f, 24.f, 32.f, 48.f, 64.f};
+  const size_t saved_hint = g_rt->cap_bin_hint;
+  float fits = 64.f;
+  for (float f : ladder) {
+    hsr_tuning cand = best;
+    cand.bin_factor = f;
+    g_rt->tuning = cand;
+    g_rt->cap_bin_hint = 0;
+    const uint64_t retries = g_rt->stats.retries;
+    int rc = g_rt->run_batch(descs, n);
+    if (rc != HSR_OK) {
+      g_rt->cap_bin_hint = saved_hint;
+      return restore(rc);
+    }
+    if (g_rt->stats.retries == retries) {
+      fits = f;
+      break;
+    }
+  }
+  g_rt->cap_bin_hint = saved_hint;
+  best.bin_factor = std::min(64.f, fits * 1.25f);
   g_rt->tuning = best;
   g_rt->profiling = saved_prof;
   if (out) *out = best;

@@ -120,6 +120,17 @@ struct TileState {
   float b0[kKeep ? NPIX : 1], b1[kKeep ? NPIX : 1], b2[kKeep ? NPIX : 1];
 };
 
+// Everything one raster CTA keeps in shared memory, in one dynamically sized block (a 32x32
+// tile needs more than the 48 KB of static shared memory; the launch opts in above that).
+template <int T, int WARPS>
+struct RasterSmem {
+  TileState<T * T> st[WARPS];
+  BatchRecs br[WARPS];
+  CandQueue cq[WARPS];
+  float u8f[256], u8n[256];
+  int32_t tbase[kSharedViews];
+};
+
 // Shade the winners of one tile and write colour, depth and prim id (fused clear writes the
 // clear values where nothing won).  S is the shader, known at compile time.  Without kept
 // weights (16x16 tiles) the winner's weights, payload index and submission come from the
@@ -149,11 +160,12 @@ __device__ __forceinline__ uint32_t shade_tile(const DView& v, const Scratch& sc
         pay = st.pay[p];
         seq = st.seq[p];
       } else if (stash) {
+        constexpr int N = T * T;
         b0 = __ldcg(stash + p);
-        b1 = __ldcg(stash + 256 + p);
-        b2 = __ldcg(stash + 512 + p);
-        pay = __ldcg(reinterpret_cast<const uint32_t*>(stash) + 768 + p);
-        seq = __ldcg(reinterpret_cast<const uint32_t*>(stash) + 1024 + p);
+        b1 = __ldcg(stash + N + p);
+        b2 = __ldcg(stash + 2 * N + p);
+        pay = __ldcg(reinterpret_cast<const uint32_t*>(stash) + 3 * N + p);
+        seq = __ldcg(reinterpret_cast<const uint32_t*>(stash) + 4 * N + p);
       } else {
         const RasterRec r = sc.recs[ri];
         cover_test(r.ax, r.ay, r.e1x, r.e1y, r.e2x, r.e2y, r.uz, ((r.view >> kRecFlagShift) & kRecExact) != 0u,
@@ -198,25 +210,22 @@ template <int T, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* __restrict__ views, Scratch sc) {
   constexpr int NPIX = T * T;
   constexpr int PPL = NPIX / 32;
-  __shared__ TileState<NPIX> sst[WARPS];
-  __shared__ BatchRecs sbr[WARPS];
-  __shared__ CandQueue scq[WARPS];
-  __shared__ float s_u8f[256], s_u8n[256];
-  __shared__ int32_t s_tbase[kSharedViews];
-  build_byte_tables(s_u8f, s_u8n);
-  const int32_t* tbase = sc.nviews <= kSharedViews ? s_tbase : nullptr;
+  extern __shared__ __align__(16) unsigned char raster_smem[];
+  RasterSmem<T, WARPS>& sm = *reinterpret_cast<RasterSmem<T, WARPS>*>(raster_smem);
+  build_byte_tables(sm.u8f, sm.u8n);
+  const int32_t* tbase = sc.nviews <= kSharedViews ? sm.tbase : nullptr;
   if (tbase)
-    for (int i = threadIdx.x; i < sc.nviews; i += blockDim.x) s_tbase[i] = views[i].tile_base;
+    for (int i = threadIdx.x; i < sc.nviews; i += blockDim.x) sm.tbase[i] = views[i].tile_base;
   __syncthreads();
-  const ByteTables bt{s_u8f, s_u8n};
+  const ByteTables bt{sm.u8f, sm.u8n};
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  TileState<NPIX>& st = sst[warp];
-  BatchRecs& br = sbr[warp];
-  CandQueue& cq = scq[warp];
+  TileState<NPIX>& st = sm.st[warp];
+  BatchRecs& br = sm.br[warp];
+  CandQueue& cq = sm.cq[warp];
   float* stash = nullptr;
   if constexpr (!TileState<NPIX>::kKeep) {
     const uint32_t gw = blockIdx.x * (uint32_t)WARPS + (uint32_t)warp;
-    if (sc.stash && gw < sc.stash_warps) stash = sc.stash + (size_t)gw * kStashFloats;
+    if (sc.stash && gw < sc.stash_warps) stash = sc.stash + (size_t)gw * (size_t)stash_floats(T);
   }
   if (sc.ctl->error & kErrNoDraw) return;
   const uint32_t nrec = min(sc.ctl->rec_count, sc.rec_cap);
@@ -273,7 +282,7 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
     const bool clear = (v.flags & HSR_DRAW_CLEAR) != 0u;
 
     if (n != 0) {  // always: the list holds the tiles with records
-#pragma unroll
+#pragma unroll 8
       for (int q = 0; q < PPL; q++) {
         const int p = lane + 32 * q;
         const int x = ox + p % T, y = oy + p / T;
@@ -353,10 +362,10 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
               st.b2[p] = b2;
             } else if (stash) {
               __stcg(stash + p, b0);
-              __stcg(stash + 256 + p, b1);
-              __stcg(stash + 512 + p, b2);
-              __stcg(reinterpret_cast<uint32_t*>(stash) + 768 + p, br.pay[j]);
-              __stcg(reinterpret_cast<uint32_t*>(stash) + 1024 + p, br.seq[j]);
+              __stcg(stash + NPIX + p, b1);
+              __stcg(stash + 2 * NPIX + p, b2);
+              __stcg(reinterpret_cast<uint32_t*>(stash) + 3 * NPIX + p, br.pay[j]);
+              __stcg(reinterpret_cast<uint32_t*>(stash) + 4 * NPIX + p, br.seq[j]);
             }
           }
           qh = (qh + cnt) & 63u;
@@ -433,7 +442,13 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
 
 template <int T, int WARPS>
 static int launch_t(const DView* views, Scratch sc, int grid, cudaStream_t s) {
-  k_raster<T, WARPS><<<grid, WARPS * 32, 0, s>>>(views, sc);
+  constexpr size_t smem = sizeof(RasterSmem<T, WARPS>);
+  if (smem > 48 * 1024) {  // opt in to more than the default 48 KB of dynamic shared memory
+    const cudaError_t e =
+        cudaFuncSetAttribute(k_raster<T, WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return (int)e;
+  }
+  k_raster<T, WARPS><<<grid, WARPS * 32, smem, s>>>(views, sc);
   return (int)cudaGetLastError();
 }
 
@@ -442,6 +457,7 @@ int launch_raster(const DView* views, int tile, Scratch sc, int grid, int warps,
   switch (tile) {
     case 8: return warps == 4 ? launch_t<8, 4>(views, sc, grid, s) : launch_t<8, 8>(views, sc, grid, s);
     case 16: return warps == 4 ? launch_t<16, 4>(views, sc, grid, s) : (int)cudaErrorInvalidValue;
+    case 32: return warps == 4 ? launch_t<32, 4>(views, sc, grid, s) : (int)cudaErrorInvalidValue;
     default: return (int)cudaErrorInvalidValue;
   }
 }

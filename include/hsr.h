@@ -246,16 +246,17 @@ HSR_API int hsr_draw_noalloc(const hsr_draw_desc* desc);
 
 /* ---- tuning ------------------------------------------------------------------------- */
 typedef struct hsr_tuning {
-  int32_t tile;           /* raster tile edge in pixels: 8 or 16                    */
+  int32_t tile;           /* raster tile edge in pixels: 8, 16 or 32 (16 and 32: 4 warps) */
   int32_t ctas_per_sm;    /* persistent raster CTAs per SM                          */
   int32_t warps_per_cta;  /* warps per raster CTA (one warp owns one tile)          */
   float bin_factor;       /* bin capacity = bin_factor * (faces + tiles) pairs      */
 } hsr_tuning;
 HSR_API int hsr_get_tuning(hsr_tuning* out);
 HSR_API int hsr_set_tuning(const hsr_tuning* in);
-/* Pick tile size, warps per CTA and CTAs per SM by timing the given batch (each candidate
- * renders it `reps` times into its targets), set them, size the bin capacity from the
- * observed (triangle, tile) pairs, and return the choice in `out` (may be NULL). */
+/* Pick tile size (8, 16, 32), warps per CTA and CTAs per SM by timing the given batch (each
+ * candidate renders it `reps` times into its targets), then search the bin capacity: the
+ * smallest bin_factor of a ladder (0.5 .. 64) with which the batch runs without overflowing,
+ * times 1.25.  Sets the choice and returns it in `out` (may be NULL). */
 HSR_API int hsr_autotune(const hsr_draw_desc* descs, int32_t n, int32_t reps, hsr_tuning* out);
 
 /* ---- failure injection for tests of the bounded device waits --------------------------

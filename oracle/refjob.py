@@ -16,18 +16,37 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 HARNESS = os.path.join(HERE, "_ref", "ref_harness")
-REF_DIR = "/root/reference/Hana-SoftwareRenderer"
+# The reference's source tree (read only): HSR_REFERENCE_DIR, else where it is unpacked on the
+# build host.  Hosts without it (the GPU hosts) use what `build` left in oracle/_ref.
+REF_DIR = os.environ.get("HSR_REFERENCE_DIR", "/root/reference/Hana-SoftwareRenderer")
+# Copies of the reference's bundled models and maps (make assets), kept out of the repository
+ASSETS = os.path.join(HERE, "_ref", "assets")
 
 
 def available() -> bool:
     return os.path.exists(HARNESS)
 
 
+def have_reference() -> bool:
+    return os.path.isdir(REF_DIR)
+
+
+def asset(model: str, suffix: str) -> str:
+    """Path of a bundled asset file in oracle/_ref/assets (e.g. asset("diablo3_pose", ".obj"))."""
+    return os.path.join(ASSETS, model, model + suffix)
+
+
+def have_assets() -> bool:
+    return all(os.path.exists(asset(m, s)) for m in ("african_head", "diablo3_pose")
+               for s in (".obj", "_diffuse.tga", "_nm_tangent.tga"))
+
+
 def build() -> bool:
-    """Build oracle/_ref from the read-only reference sources when they are present."""
-    if not os.path.isdir(REF_DIR):
+    """Build oracle/_ref (the reference's draw path headless, and the copies of its bundled
+    assets) from the read-only reference sources when they are present."""
+    if not have_reference():
         return False
-    subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "ref", "assets", f"REF={REF_DIR}"], check=True)
     return available()
 
 
@@ -71,18 +90,20 @@ def read_out(path: str) -> dict:
     return out
 
 
-def run(frame, shader: int | None = None, obj_mesh=None, workdir: str | None = None) -> dict:
+def run(frame, shader: int | None = None, obj_mesh=None, workdir: str | None = None, obj_path: str | None = None) -> dict:
     """Render one frame with the reference.  ``obj_mesh`` overrides the mesh written to
-    the OBJ (used for the per-face-uv prim-id run)."""
+    the OBJ (used for the per-face-uv prim-id run); ``obj_path`` draws an existing OBJ file
+    as Model::Model reads it (a bundled asset, with its own normals)."""
     from hsr import scenes  # noqa: WPS433 (harness-side import)
 
-    if obj_mesh is None and (frame.shader if shader is None else shader) == scenes.FLAT:
+    if obj_mesh is None and obj_path is None and (frame.shader if shader is None else shader) == scenes.FLAT:
         obj_mesh = scenes.prim_id_mesh(frame.mesh)  # FLAT == PrimIdShader on per-face uvs
     own = workdir is None
     wd = workdir or tempfile.mkdtemp(prefix="hsrref_")
     try:
-        obj = os.path.join(wd, "mesh.obj")
-        scenes.write_obj(obj_mesh if obj_mesh is not None else frame.mesh, obj)
+        obj = obj_path or os.path.join(wd, "mesh.obj")
+        if obj_path is None:
+            scenes.write_obj(obj_mesh if obj_mesh is not None else frame.mesh, obj)
         job = os.path.join(wd, "job.bin")
         out = os.path.join(wd, "out.bin")
         write_job(job, frame, obj, shader)

@@ -131,6 +131,70 @@ def fixtures():
     return out
 
 
+# The reference's bundled models in the configuration its application renders them
+# (main.cpp:7-8: a 1000x600 frame; camera.h:8-9: eye (0, 0, 2) looking at the origin; the light
+# at (2, 2, 2), scene.cpp:7; Material White / White / gloss 50 / bump 1, scene.cpp:81-84;
+# the shadow map a RenderBuffer of the frame's size, scene.h:78), with the shaders of its
+# shader list (scene.cpp:87-97).  The first is the published configuration: diablo3_pose,
+# NormalMapShader with the shadow pass.
+ASSET_SCENES = (("diablo3_pose", scenes.NORMALMAP, True), ("african_head", scenes.NORMALMAP, True),
+                ("african_head", scenes.BLINN, False), ("diablo3_pose", scenes.TOON, False))
+ASSET_W, ASSET_H = 1000, 600
+
+
+def asset_frame(model: str, shader: int, shadow: bool) -> scenes.Frame:
+    """The frame of one bundled model: mesh arrays as Model::Model parses the OBJ (for the
+    prim-id run), maps as TGAImage reads them with Model::load_texture's flip."""
+    import hsr
+
+    pos, nrm, uv, faces = hsr.obj_read(refjob.asset(model, ".obj"))
+    mesh = scenes.Mesh(pos, nrm, uv, faces)
+    diffuse = scenes.Texture(refjob.ref_tga_read(refjob.asset(model, "_diffuse.tga"), True))
+    normal = scenes.Texture(refjob.ref_tga_read(refjob.asset(model, "_nm_tangent.tga"), True))
+    sd = U.shader_data((0.0, 0.0, 2.0), ASSET_W, ASSET_H, enable_shadow=shadow)
+    return scenes.Frame(mesh, shader, sd, ASSET_W, ASSET_H, diffuse=diffuse, normal=normal,
+                        shadow_size=(ASSET_W, ASSET_H) if shadow else (0, 0),
+                        name=f"asset_{model}_{scenes.SHADER_NAMES[shader]}{'_shadow' if shadow else ''}")
+
+
+def asset_sha256(model: str) -> dict:
+    import hashlib
+
+    return {s: hashlib.sha256(open(refjob.asset(model, s), "rb").read()).hexdigest()
+            for s in (".obj", "_diffuse.tga", "_nm_tangent.tga")}
+
+
+def save_asset(model: str, shader: int, shadow: bool, path: str) -> dict:
+    """Outputs only (the assets are not copied into the repository): the reference's draw of
+    the model's own OBJ, the prim ids from the PrimIdShader run on the same positions, the
+    ShaderData bits, and the SHA-256 of each asset file the frame reads."""
+    import json
+
+    frame = asset_frame(model, shader, shadow)
+    ref = refjob.run(frame, obj_path=refjob.asset(model, ".obj"))
+    ids = refjob.run_prim_ids(frame)
+    arrays = {
+        "name": np.array(frame.name), "model": np.array(model), "shader": np.int32(shader),
+        "width": np.int32(frame.width), "height": np.int32(frame.height),
+        "shadow_size": np.array(frame.shadow_size, np.int32),
+        "clear_rgba": np.array(frame.clear_rgba, np.uint8), "clear_depth": np.float32(frame.clear_depth),
+        "shadow_clear_rgba": np.array(frame.shadow_clear_rgba, np.uint8),
+        "shadow_clear_depth": np.float32(frame.shadow_clear_depth),
+        "sd": np.frombuffer(np.ascontiguousarray(frame.sd).tobytes(), np.uint8),
+        "sha256": np.array(json.dumps(asset_sha256(model))),
+    }
+    info = {}
+    for k, v in ref.items():
+        if not (ids[k]["depth"].view(np.uint32) == v["depth"].view(np.uint32)).all():
+            raise RuntimeError(f"{frame.name}/{k}: prim-id run changed coverage or depth")
+        arrays[f"{k}_depth"] = v["depth"]
+        arrays[f"{k}_color"] = v["color"]
+        arrays[f"{k}_prim"] = ids[k]["prim"]
+        info[k] = int((ids[k]["prim"] > 0).sum())
+    np.savez_compressed(path, **arrays)
+    return info
+
+
 def save(frame, path: str) -> dict:
     ref = refjob.run(frame)
     ids = refjob.run_prim_ids(frame)
@@ -205,12 +269,22 @@ def camera(path: str) -> None:
 
 
 def main() -> None:
-    """`make_golden.py` writes every fixture; `make_golden.py frames|matrices|camera ...` only
-    the named groups."""
+    """`make_golden.py` writes every fixture; `make_golden.py frames|matrices|camera|assets ...`
+    only the named groups (assets: outputs of the bundled models, under tests/golden/assets)."""
     if not refjob.build():
         raise SystemExit("reference sources not found; fixtures can only be generated where they exist")
-    want = set(sys.argv[1:]) or {"frames", "matrices", "camera"}
+    want = set(sys.argv[1:]) or {"frames", "matrices", "camera", "assets"}
     total = 0
+    if "assets" in want:
+        if not refjob.have_assets():
+            raise SystemExit("bundled assets not copied to oracle/_ref/assets (make -C oracle assets)")
+        os.makedirs(os.path.join(HERE, "assets"), exist_ok=True)
+        for model, shader, shadow in ASSET_SCENES:
+            p = os.path.join(HERE, "assets", f"{model}_{scenes.SHADER_NAMES[shader]}{'_shadow' if shadow else ''}.npz")
+            info = save_asset(model, shader, shadow, p)
+            sz = os.path.getsize(p)
+            total += sz
+            print(f"{os.path.basename(p):40s} covered={info} {sz/1024:.0f} KiB")
     if "frames" in want:
         for fr in fixtures():
             p = os.path.join(HERE, fr.name + ".npz")

@@ -11,6 +11,45 @@ from hsr import scenes, uniforms as U
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
+ASSET_GOLDEN = os.path.join(GOLDEN, "assets")
+
+
+def asset_names() -> list[str]:
+    return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(ASSET_GOLDEN, "*.npz")))
+
+
+def load_asset(name: str):
+    """A fixture of one of the reference's bundled models (tests/golden/make_golden.py assets).
+    Returns (meta, expected): meta holds the model name, shader, sizes, clears, the ShaderData
+    record and the SHA-256 of each asset file; expected[pass] = {depth, color, prim}."""
+    import json
+
+    z = np.load(os.path.join(ASSET_GOLDEN, name + ".npz"))
+    meta = {"model": str(z["model"]), "shader": int(z["shader"]), "width": int(z["width"]),
+            "height": int(z["height"]), "shadow_size": tuple(int(v) for v in z["shadow_size"]),
+            "clear_rgba": tuple(int(v) for v in z["clear_rgba"]), "clear_depth": float(z["clear_depth"]),
+            "shadow_clear_rgba": tuple(int(v) for v in z["shadow_clear_rgba"]),
+            "shadow_clear_depth": float(z["shadow_clear_depth"]),
+            "sd": np.frombuffer(z["sd"].tobytes(), U.SHADER_DATA_DTYPE).reshape(()),
+            "sha256": json.loads(str(z["sha256"]))}
+    exp = {}
+    for k in ("main", "shadow"):
+        if f"{k}_depth" in z:
+            exp[k] = {"depth": z[f"{k}_depth"], "color": z[f"{k}_color"], "prim": z[f"{k}_prim"]}
+    return meta, exp
+
+
+def asset_files_match(meta: dict, path_of) -> bool:
+    """The asset files at path_of(model, suffix) are the ones the fixture was made from."""
+    import hashlib
+
+    for suffix, digest in meta["sha256"].items():
+        p = path_of(meta["model"], suffix)
+        if not os.path.exists(p) or hashlib.sha256(open(p, "rb").read()).hexdigest() != digest:
+            return False
+    return True
+
+
 def names() -> list[str]:
     return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
 

@@ -16,7 +16,7 @@ import refjob
 import tga_files
 from hsr import scenes
 
-ASSETS = "/root/reference/Hana-SoftwareRenderer/assets"
+ASSETS = os.path.join(refjob.REF_DIR, "assets")
 HAVE_REF = refjob.available() and os.path.isdir(ASSETS)
 needs_ref = pytest.mark.skipif(not HAVE_REF, reason="reference sources / assets not present on this host")
 

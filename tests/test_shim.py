@@ -6,16 +6,18 @@ import subprocess
 
 import pytest
 
+import refjob
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference/Hana-SoftwareRenderer"
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference sources not present on this host")
+@pytest.mark.skipif(not refjob.have_reference(), reason="reference sources not present on this host")
 def test_shim_links_into_the_reference_build():
     import build_lib
 
     build_lib.build()
-    r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "shim"], capture_output=True, text=True)
+    r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "shim", f"REF={refjob.REF_DIR}"],
+                       capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     exe = os.path.join(ROOT, "oracle", "_ref", "ref_harness_gpu")
     assert os.path.exists(exe)
