@@ -484,6 +484,69 @@ def run_soup(args) -> dict:
     return res
 
 
+def run_noclear(args) -> dict:
+    """The cost of reading a target's prior contents in the raster: the 1920x1080 frame's main
+    pass drawn with the fused clear (the raster reads nothing of the target) and drawn into a
+    target cleared beforehand to the same values without the clear flag (each visited tile
+    loads its prior depth, each shaded pixel its prior alpha).  Both give the same pixels; the
+    raster-time difference bounds what staging the prior tile contents could save."""
+    import torch
+
+    import hsr
+    from hsr import frame as hframe
+    from hsr import scenes
+
+    fr = scenes.displaced_frame()
+    g = hframe.GpuFrame(fr)
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    hsr.set_profiling(True)
+    main = g.descs[-1]
+    noclear = hsr.DrawDesc.from_buffer_copy(main)
+    noclear._keep = main._keep  # noqa: SLF001  the uniforms stay referenced
+    noclear.flags = 0
+    res = {}
+    for name, desc in (("fused_clear", main), ("prior_contents", noclear)):
+        kms = []
+        for i in range(3 + args.steps):
+            if desc is noclear:
+                g.main.clear(fr.clear_rgba, fr.clear_depth)
+            flush.zero_()
+            torch.cuda.synchronize()
+            hsr.draw_batch(g.descs[:-1] + [desc])
+            if i >= 3:
+                kms.append(hsr.last_timing()["kernel_ms"]["raster"])
+        res[name] = {"raster_ms": round(statistics.mean(kms), 4)}
+    hsr.set_profiling(False)
+    g.release()
+    res["difference_ms"] = round(res["prior_contents"]["raster_ms"] - res["fused_clear"]["raster_ms"], 4)
+    res["workload"] = FRAME_WORKLOAD
+    return res
+
+
+def run_serve_small(args) -> dict:
+    """Profiling case of the serving workload that fits a few GB of device memory: the 16
+    resident meshes and ONE batch of 8 requests (320-327 of the stream), drawn 3 times with tile
+    16, 4 warps, 8 CTAs per SM; returns the last draw's timing and counts."""
+    import hsr
+    from hsr import serve as hserve
+
+    pool, tex, reqs = serve_inputs(328)
+    reqs = reqs[320:328]
+    rp = hserve.ResidentPool(pool, tex)
+    hsr.set_tuning(tile=16, warps_per_cta=4, ctas_per_sm=8, bin_factor=4.0)
+    hsr.set_profiling(True)
+    vb = hserve.ViewBatch(rp, reqs)
+    for _ in range(3):
+        vb.draw_all()
+    t = hsr.last_timing()
+    hsr.set_profiling(False)
+    vb.release()
+    rp.release()
+    return {"workload": "serving pool, one batch of requests 320-327, drawn 3 times",
+            "batch_ms": round(t["batch_ms"], 4), "kernel_ms": {k: round(v, 4) for k, v in t["kernel_ms"].items()},
+            "counts": {k: int(t[k]) for k in COUNT_KEYS}}
+
+
 def run_views(args) -> dict:
     """64 views in one launch sequence: replayed CUDA graph vs one hsr_draw_batch vs one view
     at a time (8 meshes of 2,048-1,310,720 triangles, 256^2-1920x1080, Blinn / NormalMap,
@@ -624,7 +687,7 @@ def main():
     ap.add_argument("--warps", type=int, default=0, help="with --tile: warps per CTA of the raster (4 or 8)")
     ap.add_argument("--ctas", type=int, default=0, help="with --tile: raster CTAs per SM")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--only", choices=["frame", "views", "soup"], default=None,
+    ap.add_argument("--only", choices=["frame", "views", "soup", "noclear", "serve_small"], default=None,
                     help="run one sub-workload alone and print its result (for profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -641,7 +704,8 @@ def main():
         if args.tile:
             hsr.set_tuning(tile=args.tile, warps_per_cta=args.warps or (4 if args.tile == 16 else 8),
                            ctas_per_sm=args.ctas or None)
-        out = {"frame": run_frame, "views": run_views, "soup": run_soup}[args.only](args)
+        out = {"frame": run_frame, "views": run_views, "soup": run_soup, "noclear": run_noclear,
+               "serve_small": run_serve_small}[args.only](args)
     else:
         out = run_ours(args, world, rank, local)
     if rank == 0 and out is not None:

@@ -106,6 +106,7 @@ struct __align__(128) DView {
   // the mesh's positions and normals as (x, y, z, 0), gathered per corner for the world
   // attributes, and which of those the view's shader reads (kWorld*)
   const float4* p4; const float4* n4;
+  const float4* pk;  // unified meshes: position, normal and uv of a vertex in one sector (else null)
   uint32_t world;
   // vertex outputs (scratch)
   float4* sv;     // [npos] screen vertex: (x/w, y/w, z/w, 1/w) or plane mask (k_vertex)

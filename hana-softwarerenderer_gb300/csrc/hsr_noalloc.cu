@@ -75,7 +75,7 @@ static int noalloc_draw(Runtime* rt, const hsr_draw_desc& d) {
   std::memset(&v, 0, sizeof(v));
   v.px = m->px; v.py = m->py; v.pz = m->pz;
   v.nx = m->nx; v.ny = m->ny; v.nz = m->nz;
-  v.p4 = m->p4; v.n4 = m->n4;
+  v.p4 = m->p4; v.n4 = m->n4; v.pk = m->pk;
   v.world = world_attrs(d.shader);
   v.uv = m->uv;
   v.fv = m->fv; v.fvt = m->fvt; v.fvn = m->fvn;

@@ -69,8 +69,8 @@ static int dalloc(void** p, size_t bytes, const char* what) {
 }
 
 MeshObj::~MeshObj() {
-  for (void* p : {(void*)px, (void*)py, (void*)pz, (void*)nx, (void*)ny, (void*)nz, (void*)p4, (void*)n4, (void*)uv,
-                  (void*)fv, (void*)fvt, (void*)fvn})
+  for (void* p : {(void*)px, (void*)py, (void*)pz, (void*)nx, (void*)ny, (void*)nz, (void*)p4, (void*)n4, (void*)pk,
+                  (void*)uv, (void*)fv, (void*)fvt, (void*)fvn})
     if (p) cudaFree(p);
 }
 TexObj::~TexObj() {
@@ -191,7 +191,7 @@ int Runtime::plan_build(const hsr_draw_desc* descs, int n, Plan& p) {
     std::memset(&v, 0, sizeof(v));
     v.px = m->px; v.py = m->py; v.pz = m->pz;
     v.nx = m->nx; v.ny = m->ny; v.nz = m->nz;
-    v.p4 = m->p4; v.n4 = m->n4;
+    v.p4 = m->p4; v.n4 = m->n4; v.pk = m->pk;
     v.world = world_attrs(d.shader);
     v.uv = m->uv;
     v.fv = m->fv; v.fvt = m->fvt; v.fvn = m->fvn;
@@ -449,6 +449,27 @@ int Runtime::run_batch(const hsr_draw_desc* descs, int n) {
   return fail(HSR_ERR_BIN_OVERFLOW, "draw batch: scratch overflow persisted after retries");
 }
 
+// The packed vertex of a mesh whose corners index positions, normals and uvs alike: vertex i
+// as (x, y, z, nx), (ny, nz, u, v) from the position, normal and uv arrays (zeros where an
+// array is shorter), so a corner's attributes are one 32-byte sector.
+__global__ void k_pack_vertices(float4* __restrict__ pk, const float4* __restrict__ p4, const float4* __restrict__ n4,
+                                const float2* __restrict__ uv, int npos, int nnrm, int nuv) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npos; i += gridDim.x * blockDim.x) {
+    const float4 p = p4[i];
+    const float4 n = i < nnrm ? n4[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2 t = i < nuv ? uv[i] : make_float2(0.f, 0.f);
+    pk[2 * i] = make_float4(p.x, p.y, p.z, n.x);
+    pk[2 * i + 1] = make_float4(n.y, n.z, t.x, t.y);
+  }
+}
+
+int launch_pack_vertices(float4* pk, const float4* p4, const float4* n4, const float2* uv, int npos, int nnrm, int nuv,
+                         cudaStream_t s) {
+  if (npos <= 0) return 0;
+  k_pack_vertices<<<std::min((npos + 255) / 256, 4096), 256, 0, s>>>(pk, p4, n4, uv, npos, nnrm, nuv);
+  return (int)cudaGetLastError();
+}
+
 // renderbuffer_clear_color / renderbuffer_clear_depth (renderbuffer.cpp:59-75) with the
 // colour given as bytes; prim ids -> 0.
 __global__ void k_clear(uint32_t* __restrict__ color, float* __restrict__ depth, uint32_t* __restrict__ prim,
@@ -599,6 +620,14 @@ int hsr_mesh_upload(const float* pos, int32_t npos, const float* nrm, int32_t nn
       for (int k = 0; k < 9; k += 3) unified = unified && f[k] == f[k + 1] && f[k] == f[k + 2];
     }
     m->unified = unified;
+    if (unified && npos > 0 && rc == HSR_OK) {
+      rc = dalloc((void**)&m->pk, sizeof(float4) * 2 * (size_t)npos, "packed vertices");
+      if (rc == HSR_OK) {
+        int kr = launch_pack_vertices(m->pk, m->p4, m->n4, m->uv, npos, nnrm, nuv, g_rt->stream);
+        cudaError_t e = kr ? (cudaError_t)kr : cudaStreamSynchronize(g_rt->stream);
+        if (e != cudaSuccess) rc = cuda_fail(e, "pack vertices");
+      }
+    }
     int4** dsts[3] = {&m->fv, &m->fvt, &m->fvn};
     std::vector<int4>* srcs[3] = {&fv, &ft, &fn};
     for (int k = 0; k < 3 && rc == HSR_OK; k++) {
@@ -630,7 +659,13 @@ int hsr_mesh_update_normals(hsr_mesh mh, const float* nrm, int32_t nnrm) {
     cudaError_t e = cudaMemcpy(dst[c], tmp.data(), sizeof(float) * N, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_fail(e, "normal upload");
   }
-  return write_xyz0(nrm, nnrm, m->n4);
+  int rc = write_xyz0(nrm, nnrm, m->n4);
+  if (rc == HSR_OK && m->pk) {  // the packed vertices carry the normals too
+    int kr = launch_pack_vertices(m->pk, m->p4, m->n4, m->uv, m->npos, m->nnrm, m->nuv, g_rt->stream);
+    cudaError_t e = kr ? (cudaError_t)kr : cudaStreamSynchronize(g_rt->stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "pack vertices");
+  }
+  return rc;
 }
 
 int hsr_mesh_release(hsr_mesh mh) {

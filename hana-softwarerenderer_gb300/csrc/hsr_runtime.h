@@ -16,6 +16,8 @@ struct MeshObj {  // Model (model.h:8-33) resident on the device
   float *px = nullptr, *py = nullptr, *pz = nullptr;
   float *nx = nullptr, *ny = nullptr, *nz = nullptr;
   float4 *p4 = nullptr, *n4 = nullptr;  // positions and normals as (x, y, z, 0)
+  float4* pk = nullptr;  // meshes whose v, vt, vn indices agree: per vertex one 32-byte sector,
+                         // (x, y, z, nx), (ny, nz, u, v)
   float2* uv = nullptr;
   int4 *fv = nullptr, *fvt = nullptr, *fvn = nullptr;
   int32_t npos = 0, nnrm = 0, nuv = 0, nfaces = 0;
@@ -125,5 +127,7 @@ int cuda_fail(cudaError_t e, const char* where);
 void mat_mul_ref(const float* a, const float* b, float* out);
 void serve_shutdown();
 int launch_clear(uint32_t* color, float* depth, uint32_t* prim, size_t n, uint32_t rgba, float d, cudaStream_t s);
+int launch_pack_vertices(float4* pk, const float4* p4, const float4* n4, const float2* uv, int npos, int nnrm, int nuv,
+                         cudaStream_t s);
 
 }  // namespace hsr

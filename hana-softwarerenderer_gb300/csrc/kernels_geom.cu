@@ -86,23 +86,29 @@ __device__ __forceinline__ float4 screen_vertex(float4 c) {
 }
 __device__ __forceinline__ bool sv_normal(float4 s) { return !(fabsf(s.x) > 1.f); }
 
-// ObjectToWorldPos (IShader.h:63-65) of position i.
-__device__ __forceinline__ float4 world_pos_of(const DView& v, int i) {
-  const float4 p = __ldg(v.p4 + i);
-  const float4 w = mat_vec(v.u.model_matrix, p.x, p.y, p.z, 1.f);
+// ObjectToWorldPos (IShader.h:63-65) of an object-space position.
+__device__ __forceinline__ float4 world_pos(const DView& v, float x, float y, float z) {
+  const float4 w = mat_vec(v.u.model_matrix, x, y, z, 1.f);
   return make_float4(w.x, w.y, w.z, 0.f);
 }
-// ObjectToWorldNormal (IShader.h:71-75) = [n, 1] * model_I of normal i, with the intensity
-// of Ground / Toon, saturate(worldN . light_dir) (IShader.cpp:8, :26), in w.
-__device__ __forceinline__ float4 world_normal_of(const DView& v, int i) {
-  const float4 n = __ldg(v.n4 + i);
+__device__ __forceinline__ float4 world_pos_of(const DView& v, int i) {
+  const float4 p = __ldg(v.p4 + i);
+  return world_pos(v, p.x, p.y, p.z);
+}
+// ObjectToWorldNormal (IShader.h:71-75) = [n, 1] * model_I of an object-space normal, with the
+// intensity of Ground / Toon, saturate(worldN . light_dir) (IShader.cpp:8, :26), in w.
+__device__ __forceinline__ float4 world_normal(const DView& v, float nx, float ny, float nz) {
   const float* m = v.u.model_matrix_I;
   F3 wn;
-  wn.x = dot4(n.x, n.y, n.z, 1.f, m[0], m[4], m[8], m[12]);
-  wn.y = dot4(n.x, n.y, n.z, 1.f, m[1], m[5], m[9], m[13]);
-  wn.z = dot4(n.x, n.y, n.z, 1.f, m[2], m[6], m[10], m[14]);
+  wn.x = dot4(nx, ny, nz, 1.f, m[0], m[4], m[8], m[12]);
+  wn.y = dot4(nx, ny, nz, 1.f, m[1], m[5], m[9], m[13]);
+  wn.z = dot4(nx, ny, nz, 1.f, m[2], m[6], m[10], m[14]);
   const F3 L = {v.u.light_dir[0], v.u.light_dir[1], v.u.light_dir[2]};
   return make_float4(wn.x, wn.y, wn.z, saturate(dot3(wn, L)));
+}
+__device__ __forceinline__ float4 world_normal_of(const DView& v, int i) {
+  const float4 n = __ldg(v.n4 + i);
+  return world_normal(v, n.x, n.y, n.z);
 }
 __device__ __forceinline__ uint32_t sv_mask(float4 s) { return sv_normal(s) ? 0xffu : __float_as_uint(s.y); }
 
@@ -439,22 +445,28 @@ constexpr int kPolyStride = kVaryings;  // floats per polygon vertex in shared m
 // indices of its next chunk while it culls the current one, so the index stream from HBM
 // overlaps the gathers and arithmetic instead of waiting at the head of every chunk.
 __device__ __forceinline__ void cull_face(const DView& v, int f, uint32_t view, int4 iv, bool& valid,
-                                          bool& needs_clip, RasterRec& r) {
+                                          bool& needs_clip, RasterRec& r, float4& rw) {
   const int pi[3] = {iv.x, iv.y, iv.z};
   float4 sv[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) sv[k] = __ldg(&v.sv[pi[k]]);
   bool accept = sv_normal(sv[0]) && sv_normal(sv[1]) && sv_normal(sv[2]);
-  if (!accept) {
+  if (accept) {
+    rw = make_float4(sv[0].w, sv[1].w, sv[2].w, 0.f);  // recip_w (graphics.cpp:333-337)
+  } else {
     const uint32_t m0 = sv_mask(sv[0]), m1 = sv_mask(sv[1]), m2 = sv_mask(sv[2]);
     if (m0 & m1 & m2 & 0x80u) {
       // all three visible, one with w < 1e-5: fast accept (graphics.cpp:140-148), divide here
       accept = true;
+      float w[3];
 #pragma unroll
       for (int k = 0; k < 3; k++) {
-        const F3 n = ndc_of(clip_of(v, pi[k]));
+        const float4 c = clip_of(v, pi[k]);
+        const F3 n = ndc_of(c);
         sv[k] = make_float4(n.x, n.y, n.z, 0.f);
+        w[k] = fd(1.f, c.w);
       }
+      rw = make_float4(w[0], w[1], w[2], 0.f);
     } else {
       needs_clip = !clip_trivially_empty(m0, m1, m2);
     }
@@ -487,12 +499,20 @@ __global__ void __launch_bounds__(kSetupThreads, 4) k_setup(const DView* __restr
     const int f = ch.begin + (int)threadIdx.x;
     bool needs_clip = false, valid = false;
     RasterRec r;
-    if (f < ch.end) cull_face(v, f, (uint32_t)ch.view, iv, valid, needs_clip, r);
+    float4 rw;
+    if (f < ch.end) cull_face(v, f, (uint32_t)ch.view, iv, valid, needs_clip, r, rw);
     const uint32_t slot = block_reserve<kSetupThreads>(valid, &sc.ctl->rec_count);
     if (valid) {
       if (slot < sc.rec_cap) {
         r.pad = kPadPending;
         store_rec(&sc.recs[slot], r);
+        if (payload_f4(v.shader) > 0) {
+          // the payload's first 32 bytes until the emit pass fills it: the corners' 1/w and
+          // the face's position indices, so that pass gathers neither again
+          float4* pre = reinterpret_cast<float4*>(&sc.pay[slot]);
+          pre[0] = rw;
+          pre[1] = make_float4(__int_as_float(iv.x), __int_as_float(iv.y), __int_as_float(iv.z), 0.f);
+        }
       } else {
         atomicOr(&sc.ctl->error, kErrRecOverflow);
       }
@@ -509,31 +529,52 @@ __global__ void __launch_bounds__(kSetupThreads, 4) k_setup(const DView* __restr
   }
 }
 
-// Payload of an unclipped face from the vertex stage's outputs (Payload layout): the corner
-// varyings of its three vertex() calls and their 1/w.
-__device__ __forceinline__ void face_payload(const DView& v, int f, int nf4, Payload& pl) {
-  const int4 iv = __ldg(&v.fv[f]);
-  int4 it = iv, in = iv;  // meshes whose v, vt and vn indices agree skip two loads
+// Payload of an unclipped face (Payload layout): the corner varyings of its three vertex()
+// calls and their 1/w.  The cull pass left the corners' 1/w and position indices in the first
+// 32 bytes of the payload slot (`pre0`, `pre1`); a mesh whose corners index positions, normals
+// and uvs alike gives each corner's attributes in one 32-byte sector (DView::pk).
+__device__ __forceinline__ void face_payload(const DView& v, int f, int nf4, float4 pre0, float4 pre1, Payload& pl) {
+  const int pi[3] = {__float_as_int(pre1.x), __float_as_int(pre1.y), __float_as_int(pre1.z)};
+  const float rw[3] = {pre0.x, pre0.y, pre0.z};
+  int4 it = make_int4(pi[0], pi[1], pi[2], 0), in = it;
   if (!v.unified) {
     if (v.uv && nf4 >= 3) it = __ldg(&v.fvt[f]);
     if (v.world & kWorldNormal) in = __ldg(&v.fvn[f]);
   }
-  const int pi[3] = {iv.x, iv.y, iv.z}, ti[3] = {it.x, it.y, it.z}, ni[3] = {in.x, in.y, in.z};
+  const int ti[3] = {it.x, it.y, it.z}, ni[3] = {in.x, in.y, in.z};
+  const bool shadow = v.shader == HSR_SHADER_SHADOW;
+  const bool need_pos = (v.world & kWorldPos) || shadow, need_nrm = (v.world & kWorldNormal) != 0u;
+  const bool need_uv = v.uv && nf4 >= 3;
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-    const float4 s = __ldg(&v.sv[pi[k]]);
-    const float4 wp = (v.world & kWorldPos) ? world_pos_of(v, pi[k]) : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 wn = (v.world & kWorldNormal) ? world_normal_of(v, ni[k]) : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float2 t = (v.uv && nf4 >= 3) ? __ldg(&v.uv[ti[k]]) : make_float2(0.f, 0.f);
-    // recip_w (graphics.cpp:333-337): from the screen vertex, or divided here for a visible
-    // vertex with w < 1e-5 (the only kind of special vertex a fast-accepted face can have)
-    float rw = s.w;
-    float4 c;
-    const bool special = !sv_normal(s);
-    if (special || v.shader == HSR_SHADER_SHADOW) c = clip_of(v, pi[k]);
-    if (special) rw = fd(1.f, c.w);
-    pl.f[k] = rw;
-    pl.f[3 + k] = v.shader == HSR_SHADER_SHADOW ? c.z : wn.w;
+    float px = 0.f, py = 0.f, pz = 0.f, nx = 0.f, ny = 0.f, nz = 0.f;
+    float2 t = make_float2(0.f, 0.f);
+    if (v.pk) {
+      if (need_pos || need_nrm) {
+        const float4 a = __ldg(&v.pk[2 * pi[k]]);
+        px = a.x; py = a.y; pz = a.z; nx = a.w;
+      }
+      if (need_nrm || need_uv) {
+        const float4 b = __ldg(&v.pk[2 * pi[k] + 1]);
+        ny = b.x; nz = b.y; t = make_float2(b.z, b.w);
+      }
+    } else {
+      if (need_pos) {
+        const float4 p = __ldg(v.p4 + pi[k]);
+        px = p.x; py = p.y; pz = p.z;
+      }
+      if (need_nrm) {
+        const float4 n = __ldg(v.n4 + ni[k]);
+        nx = n.x; ny = n.y; nz = n.z;
+      }
+      if (need_uv) t = __ldg(&v.uv[ti[k]]);
+    }
+    const float4 wp = (v.world & kWorldPos) ? world_pos(v, px, py, pz) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 wn = need_nrm ? world_normal(v, nx, ny, nz) : make_float4(0.f, 0.f, 0.f, 0.f);
+    if (!need_uv) t = make_float2(0.f, 0.f);
+    pl.f[k] = rw[k];
+    // ShadowShader's interpolated clip z (ObjectToViewPos, IShader.cpp:170-174), else intensity
+    pl.f[3 + k] = shadow ? mat_vec(v.mvp, px, py, pz, 1.f).z : wn.w;
     pl.f[6 + 2 * k] = t.x;
     pl.f[7 + 2 * k] = t.y;
     pl.f[12 + 3 * k] = wn.x; pl.f[13 + 3 * k] = wn.y; pl.f[14 + 3 * k] = wn.z;
@@ -570,7 +611,10 @@ __global__ void __launch_bounds__(kSetupThreads, 4) k_emit(const DView* __restri
       if (valid) {
         v = views + (r.view & kRecViewMask);
         nf4 = payload_f4(v->shader);
-        if (nf4 > 0) face_payload(*v, (int)(r.seq >> 4), nf4, pl);
+        if (nf4 > 0) {
+          const float4* pre = reinterpret_cast<const float4*>(&sc.pay[i]);
+          face_payload(*v, (int)(r.seq >> 4), nf4, pre[0], pre[1], pl);
+        }
       }
     }
     int tx0, ty0, ntw, nt = 0;
