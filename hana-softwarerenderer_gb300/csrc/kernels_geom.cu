@@ -445,28 +445,22 @@ constexpr int kPolyStride = kVaryings;  // floats per polygon vertex in shared m
 // indices of its next chunk while it culls the current one, so the index stream from HBM
 // overlaps the gathers and arithmetic instead of waiting at the head of every chunk.
 __device__ __forceinline__ void cull_face(const DView& v, int f, uint32_t view, int4 iv, bool& valid,
-                                          bool& needs_clip, RasterRec& r, float4& rw) {
+                                          bool& needs_clip, RasterRec& r) {
   const int pi[3] = {iv.x, iv.y, iv.z};
   float4 sv[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) sv[k] = __ldg(&v.sv[pi[k]]);
   bool accept = sv_normal(sv[0]) && sv_normal(sv[1]) && sv_normal(sv[2]);
-  if (accept) {
-    rw = make_float4(sv[0].w, sv[1].w, sv[2].w, 0.f);  // recip_w (graphics.cpp:333-337)
-  } else {
+  if (!accept) {
     const uint32_t m0 = sv_mask(sv[0]), m1 = sv_mask(sv[1]), m2 = sv_mask(sv[2]);
     if (m0 & m1 & m2 & 0x80u) {
       // all three visible, one with w < 1e-5: fast accept (graphics.cpp:140-148), divide here
       accept = true;
-      float w[3];
 #pragma unroll
       for (int k = 0; k < 3; k++) {
-        const float4 c = clip_of(v, pi[k]);
-        const F3 n = ndc_of(c);
+        const F3 n = ndc_of(clip_of(v, pi[k]));
         sv[k] = make_float4(n.x, n.y, n.z, 0.f);
-        w[k] = fd(1.f, c.w);
       }
-      rw = make_float4(w[0], w[1], w[2], 0.f);
     } else {
       needs_clip = !clip_trivially_empty(m0, m1, m2);
     }
@@ -499,20 +493,12 @@ __global__ void __launch_bounds__(kSetupThreads, 4) k_setup(const DView* __restr
     const int f = ch.begin + (int)threadIdx.x;
     bool needs_clip = false, valid = false;
     RasterRec r;
-    float4 rw;
-    if (f < ch.end) cull_face(v, f, (uint32_t)ch.view, iv, valid, needs_clip, r, rw);
+    if (f < ch.end) cull_face(v, f, (uint32_t)ch.view, iv, valid, needs_clip, r);
     const uint32_t slot = block_reserve<kSetupThreads>(valid, &sc.ctl->rec_count);
     if (valid) {
       if (slot < sc.rec_cap) {
         r.pad = kPadPending;
         store_rec(&sc.recs[slot], r);
-        if (payload_f4(v.shader) > 0) {
-          // the payload's first 32 bytes until the emit pass fills it: the corners' 1/w and
-          // the face's position indices, so that pass gathers neither again
-          float4* pre = reinterpret_cast<float4*>(&sc.pay[slot]);
-          pre[0] = rw;
-          pre[1] = make_float4(__int_as_float(iv.x), __int_as_float(iv.y), __int_as_float(iv.z), 0.f);
-        }
       } else {
         atomicOr(&sc.ctl->error, kErrRecOverflow);
       }
@@ -529,24 +515,23 @@ __global__ void __launch_bounds__(kSetupThreads, 4) k_setup(const DView* __restr
   }
 }
 
-// Payload of an unclipped face (Payload layout): the corner varyings of its three vertex()
-// calls and their 1/w.  The cull pass left the corners' 1/w and position indices in the first
-// 32 bytes of the payload slot (`pre0`, `pre1`); a mesh whose corners index positions, normals
-// and uvs alike gives each corner's attributes in one 32-byte sector (DView::pk).
-__device__ __forceinline__ void face_payload(const DView& v, int f, int nf4, float4 pre0, float4 pre1, Payload& pl) {
-  const int pi[3] = {__float_as_int(pre1.x), __float_as_int(pre1.y), __float_as_int(pre1.z)};
-  const float rw[3] = {pre0.x, pre0.y, pre0.z};
-  int4 it = make_int4(pi[0], pi[1], pi[2], 0), in = it;
+// Payload of an unclipped face from the vertex stage's outputs (Payload layout): the corner
+// varyings of its three vertex() calls and their 1/w.  A mesh whose corners index positions,
+// normals and uvs alike gives each corner's attributes in one 32-byte sector (DView::pk).
+__device__ __forceinline__ void face_payload(const DView& v, int f, int nf4, Payload& pl) {
+  const int4 iv = __ldg(&v.fv[f]);
+  int4 it = iv, in = iv;  // meshes whose v, vt and vn indices agree skip two loads
   if (!v.unified) {
     if (v.uv && nf4 >= 3) it = __ldg(&v.fvt[f]);
     if (v.world & kWorldNormal) in = __ldg(&v.fvn[f]);
   }
-  const int ti[3] = {it.x, it.y, it.z}, ni[3] = {in.x, in.y, in.z};
+  const int pi[3] = {iv.x, iv.y, iv.z}, ti[3] = {it.x, it.y, it.z}, ni[3] = {in.x, in.y, in.z};
   const bool shadow = v.shader == HSR_SHADER_SHADOW;
   const bool need_pos = (v.world & kWorldPos) || shadow, need_nrm = (v.world & kWorldNormal) != 0u;
   const bool need_uv = v.uv && nf4 >= 3;
 #pragma unroll
   for (int k = 0; k < 3; k++) {
+    const float4 s = __ldg(&v.sv[pi[k]]);
     float px = 0.f, py = 0.f, pz = 0.f, nx = 0.f, ny = 0.f, nz = 0.f;
     float2 t = make_float2(0.f, 0.f);
     if (v.pk) {
@@ -572,7 +557,11 @@ __device__ __forceinline__ void face_payload(const DView& v, int f, int nf4, flo
     const float4 wp = (v.world & kWorldPos) ? world_pos(v, px, py, pz) : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 wn = need_nrm ? world_normal(v, nx, ny, nz) : make_float4(0.f, 0.f, 0.f, 0.f);
     if (!need_uv) t = make_float2(0.f, 0.f);
-    pl.f[k] = rw[k];
+    // recip_w (graphics.cpp:333-337): from the screen vertex, or divided here for a visible
+    // vertex with w < 1e-5 (the only kind of special vertex a fast-accepted face can have)
+    float rw = s.w;
+    if (!sv_normal(s)) rw = fd(1.f, clip_of(v, pi[k]).w);
+    pl.f[k] = rw;
     // ShadowShader's interpolated clip z (ObjectToViewPos, IShader.cpp:170-174), else intensity
     pl.f[3 + k] = shadow ? mat_vec(v.mvp, px, py, pz, 1.f).z : wn.w;
     pl.f[6 + 2 * k] = t.x;
@@ -611,10 +600,7 @@ __global__ void __launch_bounds__(kSetupThreads, 4) k_emit(const DView* __restri
       if (valid) {
         v = views + (r.view & kRecViewMask);
         nf4 = payload_f4(v->shader);
-        if (nf4 > 0) {
-          const float4* pre = reinterpret_cast<const float4*>(&sc.pay[i]);
-          face_payload(*v, (int)(r.seq >> 4), nf4, pre[0], pre[1], pl);
-        }
+        if (nf4 > 0) face_payload(*v, (int)(r.seq >> 4), nf4, pl);
       }
     }
     int tx0, ty0, ntw, nt = 0;
