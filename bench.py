@@ -547,6 +547,28 @@ def run_serve_small(args) -> dict:
             "counts": {k: int(t[k]) for k in COUNT_KEYS}}
 
 
+def run_soup_small(args) -> dict:
+    """Profiling case of the depth-order stress workload that fits a few GB: the soup at a
+    quarter of its size (1,000,000 triangles at 1920x1080: the same triangles per pixel, edge
+    lengths and depth complexity), drawn 3 times with tile 16, 4 warps, 8 CTAs per SM."""
+    import hsr
+    from hsr import frame as hframe
+    from hsr import scenes
+
+    fr = scenes.soup_frame(1_000_000, 1920, 1080)
+    g = hframe.GpuFrame(fr)
+    hsr.set_tuning(tile=16, warps_per_cta=4, ctas_per_sm=8, bin_factor=4.0)
+    hsr.set_profiling(True)
+    for _ in range(3):
+        g.render()
+    t = hsr.last_timing()
+    hsr.set_profiling(False)
+    g.release()
+    return {"workload": "triangle soup, 1,000,000 tris at 1920x1080 (a quarter of the stress frame), drawn 3 times",
+            "batch_ms": round(t["batch_ms"], 4), "kernel_ms": {k: round(v, 4) for k, v in t["kernel_ms"].items()},
+            "counts": {k: int(t[k]) for k in COUNT_KEYS}}
+
+
 def run_views(args) -> dict:
     """64 views in one launch sequence: replayed CUDA graph vs one hsr_draw_batch vs one view
     at a time (8 meshes of 2,048-1,310,720 triangles, 256^2-1920x1080, Blinn / NormalMap,
@@ -687,7 +709,7 @@ def main():
     ap.add_argument("--warps", type=int, default=0, help="with --tile: warps per CTA of the raster (4 or 8)")
     ap.add_argument("--ctas", type=int, default=0, help="with --tile: raster CTAs per SM")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--only", choices=["frame", "views", "soup", "noclear", "serve_small"], default=None,
+    ap.add_argument("--only", choices=["frame", "views", "soup", "noclear", "serve_small", "soup_small"], default=None,
                     help="run one sub-workload alone and print its result (for profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -705,7 +727,7 @@ def main():
             hsr.set_tuning(tile=args.tile, warps_per_cta=args.warps or (4 if args.tile == 16 else 8),
                            ctas_per_sm=args.ctas or None)
         out = {"frame": run_frame, "views": run_views, "soup": run_soup, "noclear": run_noclear,
-               "serve_small": run_serve_small}[args.only](args)
+               "serve_small": run_serve_small, "soup_small": run_soup_small}[args.only](args)
     else:
         out = run_ours(args, world, rank, local)
     if rank == 0 and out is not None:

@@ -136,7 +136,7 @@ __host__ __device__ inline uint32_t world_attrs(int shader) {
                    shader == HSR_SHADER_BLINN || shader == HSR_SHADER_NORMALMAP;
   return (pos ? kWorldPos : 0u) | (nrm ? kWorldNormal : 0u);
 }
-constexpr int kSetupChunk = 256;    // faces per setup chunk (one per thread of a block)
+constexpr int kSetupChunk = 128;    // faces per setup chunk (one per thread of a block)
 constexpr int kClearChunk = 1024;   // pixels per clear chunk (32 per lane of a warp)
 constexpr int64_t kMaxBatchTiles = (int64_t)1 << 26;  // tiles of one launch sequence (scan word)
 static_assert(offsetof(DView, prim_base) + sizeof(uint32_t) <= 128, "per-tile fields must share one line");

@@ -174,7 +174,7 @@ static int noalloc_draw(Runtime* rt, const hsr_draw_desc& d) {
   e = cudaMemsetAsync(dev + o_zero, 0, zero_bytes, s);  // counters start at zero every call
   if (e != cudaSuccess) return cuda_fail(e, "draw_noalloc: clear counters");
   int kr = launch_vertex(dview, 1, nvch, rt->num_sms * 8, s);
-  if (!kr) kr = launch_setup(dview, 1, nsch, sc, rt->num_sms * 4, s);
+  if (!kr) kr = launch_setup(dview, 1, nsch, sc, rt->num_sms * 8, s);
   if (!kr) kr = launch_emit(dview, T, sc, rt->num_sms * 8, s);
   if (!kr) kr = launch_post(dview, T, sc, rt->num_sms * 4, s);
   if (!kr) kr = launch_big(dview, T, sc, rt->num_sms * 2, s);

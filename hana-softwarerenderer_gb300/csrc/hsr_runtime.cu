@@ -331,7 +331,7 @@ int Plan::enqueue(cudaStream_t s, int num_sms, const hsr_tuning& tu, cudaEvent_t
   int kr = launch_vertex(dviews, n, nvch, num_sms * 8, s);
   if (kr) return cuda_fail((cudaError_t)kr, "vertex kernel");
   mark(2);
-  kr = launch_setup(dviews, n, nsch, sc, num_sms * 4, s);
+  kr = launch_setup(dviews, n, nsch, sc, num_sms * 8, s);
   if (kr) return cuda_fail((cudaError_t)kr, "setup kernel");
   mark(3);
   kr = launch_emit(dviews, tile, sc, num_sms * 8, s);

@@ -430,7 +430,8 @@ __device__ __forceinline__ bool clip_trivially_empty(uint32_t m0, uint32_t m1, u
   return false;
 }
 
-constexpr int kSetupThreads = 256;
+constexpr int kSetupThreads = kSetupChunk;  // one face per thread; a block's barriers span 4 warps
+constexpr int kEmitThreads = 256;
 constexpr int kPolyStride = kVaryings;  // floats per polygon vertex in shared memory
 
 
@@ -441,7 +442,7 @@ constexpr int kPolyStride = kVaryings;  // floats per polygon vertex in shared m
 // here, so the per-record work runs in k_emit on dense warps instead of on the few lanes
 // that survive in each warp of this pass.
 //
-// Persistent: block b takes chunks b, b + grid, ... (256 faces each) and loads the face
+// Persistent: block b takes chunks b, b + grid, ... (kSetupChunk faces each) and loads the face
 // indices of its next chunk while it culls the current one, so the index stream from HBM
 // overlaps the gathers and arithmetic instead of waiting at the head of every chunk.
 __device__ __forceinline__ void cull_face(const DView& v, int f, uint32_t view, int4 iv, bool& valid,
@@ -470,7 +471,7 @@ __device__ __forceinline__ void cull_face(const DView& v, int f, uint32_t view, 
                       (uint32_t)f << 4, view, r);
 }
 
-__global__ void __launch_bounds__(kSetupThreads, 4) k_setup(const DView* __restrict__ views, int nviews,
+__global__ void __launch_bounds__(kSetupThreads, 8) k_setup(const DView* __restrict__ views, int nviews,
                                                          int nchunks, Scratch sc) {
   __shared__ int32_t s_base[kSharedViews];
   const int32_t* base = share_bases(views, nviews, s_base, SchBase());
@@ -577,7 +578,7 @@ __device__ __forceinline__ void face_payload(const DView& v, int f, int nf4, Pay
 // shading payload, the tile counts, and the hand-over of huge triangles to k_big (their
 // slot becomes a hole the binning skips).  Grid-stride with warp-uniform trip counts, so
 // the warp collectives of append_small see every lane.
-__global__ void __launch_bounds__(kSetupThreads, 4) k_emit(const DView* __restrict__ views, int T, Scratch sc) {
+__global__ void __launch_bounds__(kEmitThreads, 4) k_emit(const DView* __restrict__ views, int T, Scratch sc) {
   const int lane = threadIdx.x & 31;
   if (sc.ctl->error & kErrCapacity) return;
   const uint32_t nrec = min(sc.ctl->rec_count, sc.rec_cap);
@@ -629,7 +630,7 @@ __global__ void __launch_bounds__(kSetupThreads, 4) k_emit(const DView* __restri
 }
 
 int launch_emit(const DView* views, int tile, Scratch sc, int grid, cudaStream_t s) {
-  k_emit<<<grid, kSetupThreads, 0, s>>>(views, tile, sc);
+  k_emit<<<grid, kEmitThreads, 0, s>>>(views, tile, sc);
   return (int)cudaGetLastError();
 }
 
