@@ -270,6 +270,7 @@ def run_ours(args, world, rank, local):
         tuned = hsr.autotune(vb.descs, reps=2)  # outside the timed region
         vb.release()
     hsr.set_profiling(True)
+    retries0 = None
 
     # ---- value: one launch sequence of 64 requests per step ------------------------------
     step_ms, kernel_ms, launches, h2d, d2h = [], {k: [] for k in hsr.KERNELS}, 0, [], []
@@ -282,6 +283,7 @@ def run_ours(args, world, rank, local):
             dist_barrier(world)
             torch.cuda.synchronize()
             sampler.start()
+            retries0 = hsr.stats()["retries"]
         flush.zero_()
         torch.cuda.synchronize()
         vb.draw_all()
@@ -299,6 +301,7 @@ def run_ours(args, world, rank, local):
             counts_sum[k] = counts_sum.get(k, 0) + int(t[k])
     torch.cuda.synchronize()
     clocks = sampler.stop()
+    retries = hsr.stats()["retries"] - (retries0 or 0)  # scratch overflows re-run inside the timed steps
     dist_barrier(world)
     frames = args.steps * BATCH
     total_s = dist_max(sum(step_ms) / 1000.0, world)
@@ -345,6 +348,7 @@ def run_ours(args, world, rank, local):
         "kernel_ms": {k: round(statistics.mean(v), 4) for k, v in kernel_ms.items()},
         "counts_per_step": {k: int(v) for k, v in counts.items()},
         "gpu_launches": launches,
+        "scratch_retries": retries,
         "clocks": clocks,
     }
 

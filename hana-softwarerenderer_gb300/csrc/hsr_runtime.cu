@@ -870,7 +870,7 @@ int hsr_host_free(void* p) {
 // CTAs per SM 1..8), keeps the fastest median device time, then searches the bin capacity:
 // the smallest factor of a ladder with which the batch runs without a bin overflow (capacity
 // hints learnt from earlier overflows set aside during the search), plus a quarter of headroom
-// for the next batches of a stream.  The batch's targets receive the renders.
+// for the next batches of a stream, and at least 1 (a bin entry per triangle and tile).  The batch's targets receive the renders.
 int hsr_autotune(const hsr_draw_desc* descs, int32_t n, int32_t reps, hsr_tuning* out) {
   RT_OR_FAIL();
   if (!descs || n <= 0 || reps <= 0) return fail(HSR_ERR_INVALID_ARG, "autotune: bad arguments");
@@ -929,7 +929,7 @@ int hsr_autotune(const hsr_draw_desc* descs, int32_t n, int32_t reps, hsr_tuning
     }
   }
   g_rt->cap_bin_hint = saved_hint;
-  best.bin_factor = std::min(64.f, fits * 1.25f);
+  best.bin_factor = std::min(64.f, std::max(1.f, fits * 1.25f));
   g_rt->tuning = best;
   g_rt->profiling = saved_prof;
   if (out) *out = best;

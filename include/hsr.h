@@ -256,7 +256,7 @@ HSR_API int hsr_set_tuning(const hsr_tuning* in);
 /* Pick tile size (8, 16, 32), warps per CTA and CTAs per SM by timing the given batch (each
  * candidate renders it `reps` times into its targets), then search the bin capacity: the
  * smallest bin_factor of a ladder (0.5 .. 64) with which the batch runs without overflowing,
- * times 1.25.  Sets the choice and returns it in `out` (may be NULL). */
+ * times 1.25 and at least 1.  Sets the choice and returns it in `out` (may be NULL). */
 HSR_API int hsr_autotune(const hsr_draw_desc* descs, int32_t n, int32_t reps, hsr_tuning* out);
 
 /* ---- failure injection for tests of the bounded device waits --------------------------
