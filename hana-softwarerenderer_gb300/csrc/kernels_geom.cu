@@ -516,11 +516,12 @@ __global__ void __launch_bounds__(kSetupThreads, 8) k_setup(const DView* __restr
   }
 }
 
-// Payload of an unclipped face from the vertex stage's outputs (Payload layout): the corner
-// varyings of its three vertex() calls and their 1/w.  A mesh whose corners index positions,
-// normals and uvs alike gives each corner's attributes in one 32-byte sector (DView::pk).
-__device__ __forceinline__ void face_payload(const DView& v, int f, int nf4, Payload& pl) {
-  const int4 iv = __ldg(&v.fv[f]);
+// Payload of an unclipped face (Payload layout): the corner varyings of its three vertex()
+// calls and their 1/w.  A mesh whose corners index positions, normals and uvs alike gives each
+// corner's attributes in one 32-byte sector (DView::pk), and the corner's 1/w is computed from
+// its position with the operations k_vertex used for the screen vertex (clip = mvp * [p, 1],
+// 1 / clip.w; graphics.cpp:333-337), so no screen vertex is gathered again.
+__device__ __forceinline__ void face_payload(const DView& v, int f, int nf4, int4 iv, Payload& pl) {
   int4 it = iv, in = iv;  // meshes whose v, vt and vn indices agree skip two loads
   if (!v.unified) {
     if (v.uv && nf4 >= 3) it = __ldg(&v.fvt[f]);
@@ -528,43 +529,35 @@ __device__ __forceinline__ void face_payload(const DView& v, int f, int nf4, Pay
   }
   const int pi[3] = {iv.x, iv.y, iv.z}, ti[3] = {it.x, it.y, it.z}, ni[3] = {in.x, in.y, in.z};
   const bool shadow = v.shader == HSR_SHADER_SHADOW;
-  const bool need_pos = (v.world & kWorldPos) || shadow, need_nrm = (v.world & kWorldNormal) != 0u;
+  const bool need_nrm = (v.world & kWorldNormal) != 0u;
   const bool need_uv = v.uv && nf4 >= 3;
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-    const float4 s = __ldg(&v.sv[pi[k]]);
-    float px = 0.f, py = 0.f, pz = 0.f, nx = 0.f, ny = 0.f, nz = 0.f;
+    float px, py, pz, nx = 0.f, ny = 0.f, nz = 0.f;
     float2 t = make_float2(0.f, 0.f);
     if (v.pk) {
-      if (need_pos || need_nrm) {
-        const float4 a = __ldg(&v.pk[2 * pi[k]]);
-        px = a.x; py = a.y; pz = a.z; nx = a.w;
-      }
+      const float4 a = __ldg(&v.pk[2 * pi[k]]);
+      px = a.x; py = a.y; pz = a.z; nx = a.w;
       if (need_nrm || need_uv) {
         const float4 b = __ldg(&v.pk[2 * pi[k] + 1]);
         ny = b.x; nz = b.y; t = make_float2(b.z, b.w);
       }
     } else {
-      if (need_pos) {
-        const float4 p = __ldg(v.p4 + pi[k]);
-        px = p.x; py = p.y; pz = p.z;
-      }
+      const float4 p = __ldg(v.p4 + pi[k]);
+      px = p.x; py = p.y; pz = p.z;
       if (need_nrm) {
         const float4 n = __ldg(v.n4 + ni[k]);
         nx = n.x; ny = n.y; nz = n.z;
       }
       if (need_uv) t = __ldg(&v.uv[ti[k]]);
     }
+    const float4 c = mat_vec(v.mvp, px, py, pz, 1.f);  // ObjectToClipPos (IShader.h:55-61)
     const float4 wp = (v.world & kWorldPos) ? world_pos(v, px, py, pz) : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 wn = need_nrm ? world_normal(v, nx, ny, nz) : make_float4(0.f, 0.f, 0.f, 0.f);
     if (!need_uv) t = make_float2(0.f, 0.f);
-    // recip_w (graphics.cpp:333-337): from the screen vertex, or divided here for a visible
-    // vertex with w < 1e-5 (the only kind of special vertex a fast-accepted face can have)
-    float rw = s.w;
-    if (!sv_normal(s)) rw = fd(1.f, clip_of(v, pi[k]).w);
-    pl.f[k] = rw;
+    pl.f[k] = fd(1.f, c.w);  // recip_w
     // ShadowShader's interpolated clip z (ObjectToViewPos, IShader.cpp:170-174), else intensity
-    pl.f[3 + k] = shadow ? mat_vec(v.mvp, px, py, pz, 1.f).z : wn.w;
+    pl.f[3 + k] = shadow ? c.z : wn.w;
     pl.f[6 + 2 * k] = t.x;
     pl.f[7 + 2 * k] = t.y;
     pl.f[12 + 3 * k] = wn.x; pl.f[13 + 3 * k] = wn.y; pl.f[14 + 3 * k] = wn.z;
@@ -601,7 +594,10 @@ __global__ void __launch_bounds__(kEmitThreads, 4) k_emit(const DView* __restric
       if (valid) {
         v = views + (r.view & kRecViewMask);
         nf4 = payload_f4(v->shader);
-        if (nf4 > 0) face_payload(*v, (int)(r.seq >> 4), nf4, pl);
+        if (nf4 > 0) {
+          const int f = (int)(r.seq >> 4);
+          face_payload(*v, f, nf4, __ldg(&v->fv[f]), pl);
+        }
       }
     }
     int tx0, ty0, ntw, nt = 0;
