@@ -630,17 +630,20 @@ int launch_emit(const DView* views, int tile, Scratch sc, int grid, cudaStream_t
   return (int)cudaGetLastError();
 }
 
-// Homogeneous clipping of one face by one warp (graphics.cpp:73-161): lane k carries
-// varying k of the polygon through Sutherland-Hodgman while every lane evaluates the plane
-// tests on the clip coordinates; lanes j < n-2 then build the fan triangles (:394-405).
-__device__ void clip_face(const DView& v, int view, int face, int T, const Scratch& sc, float* A, float* B) {
-  const int lane = threadIdx.x & 31;
-  if (lane < 3) {
+// Homogeneous clipping (graphics.cpp:73-161), two faces per warp: each half-warp clips its own
+// face (`active`), lane k of the half carrying varying k of the polygon through
+// Sutherland-Hodgman while every lane evaluates the plane tests on the clip coordinates; lanes
+// j < n-2 of the half then build the fan triangles (:394-405).  The halves run the same
+// instructions, each masked to its own polygon; every __syncwarp is reached by all 32 lanes.
+__device__ void clip_face(bool active, const DView& v, int view, int face, int T, const Scratch& sc, float* A,
+                          float* B) {
+  const int lane = threadIdx.x & 31, hl = lane & 15;
+  if (active && hl < 3) {
     const int4 iv = __ldg(&v.fv[face]), it = __ldg(&v.fvt[face]), in = __ldg(&v.fvn[face]);
-    const int pi = lane == 0 ? iv.x : (lane == 1 ? iv.y : iv.z);
-    const int ti = lane == 0 ? it.x : (lane == 1 ? it.y : it.z);
-    const int ni = lane == 0 ? in.x : (lane == 1 ? in.y : in.z);
-    float* o = A + lane * kPolyStride;
+    const int pi = hl == 0 ? iv.x : (hl == 1 ? iv.y : iv.z);
+    const int ti = hl == 0 ? it.x : (hl == 1 ? it.y : it.z);
+    const int ni = hl == 0 ? in.x : (hl == 1 ? in.y : in.z);
+    float* o = A + hl * kPolyStride;
     const float4 c = clip_of(v, pi);
     o[0] = c.x; o[1] = c.y; o[2] = c.z; o[3] = c.w;
     const float4 wp = (v.world & kWorldPos) ? world_pos_of(v, pi) : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -651,40 +654,42 @@ __device__ void clip_face(const DView& v, int view, int face, int T, const Scrat
     o[10] = t.x; o[11] = t.y; o[12] = wn.w;
   }
   __syncwarp();
-  int n = 3;
+  int n = active ? 3 : 0;
   float* src = A;
   float* dst = B;
 #pragma unroll
   for (int plane = PW; plane <= NZ; plane++) {
-    if (n < 3) break;
+    // a polygon with fewer than 3 vertices is dropped (its later planes are skipped)
     int m = 0;
-    for (int i = 0; i < n; i++) {
-      const float* prev = src + (i == 0 ? n - 1 : i - 1) * kPolyStride;
-      const float* curr = src + i * kPolyStride;
-      const bool pin = inside_plane(prev, plane), cin = inside_plane(curr, plane);
-      if (pin != cin) {
-        const float t = intersect_ratio(prev, curr, plane);
-        if (lane < kVaryings) dst[m * kPolyStride + lane] = fa(prev[lane], fm(fs(curr[lane], prev[lane]), t));
-        m++;
+    if (n >= 3) {
+      for (int i = 0; i < n; i++) {
+        const float* prev = src + (i == 0 ? n - 1 : i - 1) * kPolyStride;
+        const float* curr = src + i * kPolyStride;
+        const bool pin = inside_plane(prev, plane), cin = inside_plane(curr, plane);
+        if (pin != cin) {
+          const float t = intersect_ratio(prev, curr, plane);
+          if (hl < kVaryings) dst[m * kPolyStride + hl] = fa(prev[hl], fm(fs(curr[hl], prev[hl]), t));
+          m++;
+        }
+        if (cin) {
+          if (hl < kVaryings) dst[m * kPolyStride + hl] = curr[hl];
+          m++;
+        }
       }
-      if (cin) {
-        if (lane < kVaryings) dst[m * kPolyStride + lane] = curr[lane];
-        m++;
-      }
+      n = m;
     }
     __syncwarp();
-    n = m;
     float* tmp = src; src = dst; dst = tmp;
   }
   bool valid = false;
   RasterRec r;
   Payload pl;
-  if (n >= 3 && lane < n - 2) {
+  if (n >= 3 && hl < n - 2) {
     const float* p0 = src;
-    const float* p1 = src + (lane + 1) * kPolyStride;
-    const float* p2 = src + (lane + 2) * kPolyStride;
+    const float* p1 = src + (hl + 1) * kPolyStride;
+    const float* p2 = src + (hl + 2) * kPolyStride;
     valid = build_rec(v, ndc_of(make_float4(p0[0], p0[1], p0[2], p0[3])), ndc_of(make_float4(p1[0], p1[1], p1[2], p1[3])),
-                      ndc_of(make_float4(p2[0], p2[1], p2[2], p2[3])), ((uint32_t)face << 4) | ((uint32_t)lane << 1) | 1u,
+                      ndc_of(make_float4(p2[0], p2[1], p2[2], p2[3])), ((uint32_t)face << 4) | ((uint32_t)hl << 1) | 1u,
                       (uint32_t)view, r);
     if (valid) make_payload(v.shader, p0, p1, p2, pl);
   }
@@ -710,26 +715,28 @@ __device__ void clip_face(const DView& v, int view, int face, int T, const Scrat
 
 constexpr int kPostThreads = 256;
 
-// Drains the clip queue of k_setup, one warp per face.  Faces are claimed one ahead, so the
-// claim's round trip overlaps the current face; the grid fills every SM (the queue is short
+// Drains the clip queue of k_setup, two faces per warp.  Face pairs are claimed one ahead, so
+// the claim's round trip overlaps the current pair; the grid fills every SM (the queue is short
 // and each face is a chain of dependent loads, so resident warps set the throughput).
 __global__ void __launch_bounds__(kPostThreads, 4) k_post(const DView* __restrict__ views, int T, Scratch sc) {
-  __shared__ float poly[kPostThreads / 32][2][16 * kPolyStride];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __shared__ float poly[kPostThreads / 32][2][2][16 * kPolyStride];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, half = lane >> 4;
   if (sc.ctl->error & kErrCapacity) return;
   const uint32_t nclip = min(sc.ctl->clip_count, sc.clip_cap);
   uint32_t item = 0, ahead = 0;
   if (lane == 0) {
-    item = atomicAdd(&sc.ctl->post_next, 1u);
-    ahead = item < nclip ? atomicAdd(&sc.ctl->post_next, 1u) : nclip;
+    item = atomicAdd(&sc.ctl->post_next, 2u);
+    ahead = item < nclip ? atomicAdd(&sc.ctl->post_next, 2u) : nclip;
   }
   item = __shfl_sync(kFull, item, 0);
   for (;;) {
     if (item >= nclip) break;
     const uint32_t next = __shfl_sync(kFull, ahead, 0);
-    if (lane == 0) ahead = next < nclip ? atomicAdd(&sc.ctl->post_next, 1u) : nclip;
-    const int2 vf = sc.clipq[item];
-    clip_face(views[vf.x], vf.x, vf.y, T, sc, poly[warp][0], poly[warp][1]);
+    if (lane == 0) ahead = next < nclip ? atomicAdd(&sc.ctl->post_next, 2u) : nclip;
+    const uint32_t mine = item + (uint32_t)half;
+    const bool active = mine < nclip;
+    const int2 vf = active ? sc.clipq[mine] : make_int2(0, 0);
+    clip_face(active, views[vf.x], vf.x, vf.y, T, sc, poly[warp][half][0], poly[warp][half][1]);
     item = next;
   }
 }
