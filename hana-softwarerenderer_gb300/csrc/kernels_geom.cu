@@ -173,34 +173,28 @@ __device__ __forceinline__ Chunk setup_chunk(const DView* views, const int32_t* 
 // ---------------------------------------------------------------------------------------
 // vertex stage
 // ---------------------------------------------------------------------------------------
-// One vertex chunk (kVertexChunk positions, 256 threads, two runs of 4 consecutive positions
-// per thread): ObjectToClipPos / ObjectToViewPos (IShader.h:55-61) -> screen vertex.  A run is
-// read with one 128-bit load per component stream (the SoA arrays are padded to a multiple of
-// 4 and a chunk starts on a multiple of 4), so each load instruction of a warp covers 512
-// contiguous bytes; the run's four screen vertices are written as four float4s.  The loads of
-// both runs are issued before any is used.
-static_assert(kVertexChunk % (4 * 256) == 0, "a vertex chunk is whole runs of 4 positions per thread");
+// One vertex chunk (kVertexChunk positions, 8 per thread, 256 threads): ObjectToClipPos /
+// ObjectToViewPos (IShader.h:55-61) -> screen vertex.
 __device__ __forceinline__ void vertex_chunk_work(const DView& v, const Chunk& ch) {
-  constexpr int kRuns = kVertexChunk / (4 * 256);
-  float4 xs[kRuns], ys[kRuns], zs[kRuns];
+  // item i = begin + threadIdx.x + 256 k: consecutive threads read consecutive floats and
+  // write consecutive float4s, so every load and store instruction of a warp is one
+  // contiguous span; the loads of a thread are issued before any is used
+  constexpr int kPer = kVertexChunk / 256;
+  const int i0 = ch.begin + (int)threadIdx.x;
+  float xs[kPer], ys[kPer], zs[kPer];
 #pragma unroll
-  for (int k = 0; k < kRuns; k++) {
-    const int i = ch.begin + 4 * ((int)threadIdx.x + 256 * k);
-    const bool in = i < ch.end;  // then i + 3 lies inside the padded arrays
-    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    xs[k] = in ? __ldg(reinterpret_cast<const float4*>(v.px + i)) : z4;
-    ys[k] = in ? __ldg(reinterpret_cast<const float4*>(v.py + i)) : z4;
-    zs[k] = in ? __ldg(reinterpret_cast<const float4*>(v.pz + i)) : z4;
+  for (int k = 0; k < kPer; k++) {
+    const int i = i0 + 256 * k;
+    const bool in = i < ch.end;
+    xs[k] = in ? __ldg(v.px + i) : 0.f;
+    ys[k] = in ? __ldg(v.py + i) : 0.f;
+    zs[k] = in ? __ldg(v.pz + i) : 0.f;
   }
 #pragma unroll
-  for (int k = 0; k < kRuns; k++) {
-    const int i = ch.begin + 4 * ((int)threadIdx.x + 256 * k);
-    const float x[4] = {xs[k].x, xs[k].y, xs[k].z, xs[k].w};
-    const float y[4] = {ys[k].x, ys[k].y, ys[k].z, ys[k].w};
-    const float z[4] = {zs[k].x, zs[k].y, zs[k].z, zs[k].w};
-#pragma unroll
-    for (int q = 0; q < 4; q++)
-      if (i + q < ch.end) v.sv[i + q] = screen_vertex(mat_vec(v.mvp, x[q], y[q], z[q], 1.f));
+  for (int k = 0; k < kPer; k++) {
+    const int i = i0 + 256 * k;
+    if (i >= ch.end) break;
+    v.sv[i] = screen_vertex(mat_vec(v.mvp, xs[k], ys[k], zs[k], 1.f));
   }
 }
 
