@@ -197,14 +197,22 @@ def kernel_bytes(t: dict) -> dict:
     }
 
 
-def ncu_traffic(workload: str, kernel: str):
-    """DRAM bytes per launch of `kernel` from the committed ncu capture of `workload`."""
+def _ncu_record(workload: str) -> dict:
     p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     if not os.path.exists(p):
-        return None
+        return {}
     with open(p) as f:
-        d = json.load(f)
-    return d.get("workloads", {}).get(workload, {}).get("dram_bytes_per_launch", {}).get(kernel)
+        return json.load(f).get("workloads", {}).get(workload, {})
+
+
+def ncu_traffic(workload: str, kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu capture of `workload`."""
+    return _ncu_record(workload).get("dram_bytes_per_launch", {}).get(kernel)
+
+
+def ncu_utilisation(workload: str, kernel: str):
+    """Issue-active and pipe utilisation of `kernel` from the committed ncu capture (or None)."""
+    return _ncu_record(workload).get("utilisation", {}).get(kernel)
 
 
 def roofline(kernel_ms: dict, counts: dict, workload: str) -> dict:
@@ -220,14 +228,19 @@ def roofline(kernel_ms: dict, counts: dict, workload: str) -> dict:
         per[k] = {"ms": round(ms, 5), "share": round(ms / total, 4) if total else 0.0,
                   "algorithmic_bytes": int(kb[k]), "achieved_gbs": round(gbs, 1),
                   "frac": round(gbs / pk["hbm_gbs"], 4), "traffic": ncu_traffic(workload, k)}
+        u = ncu_utilisation(workload, k)
+        if u:
+            per[k]["ncu"] = u
     top = max(mean_k, key=mean_k.get)
     return {"kernel": top, "bound": "hbm", "achieved": per[top]["achieved_gbs"], "peak": pk["hbm_gbs"],
             "peak_source": pk["source"], "unit": "GB/s", "frac": per[top]["frac"],
             "algorithmic_bytes": per[top]["algorithmic_bytes"], "ms": per[top]["ms"], "traffic": per[top]["traffic"],
+            "issue": per[top].get("ncu"),
             "kernels": per,
             "note": "the kernel with the largest share of the step; every kernel's share, algorithmic bytes and "
-                    "fraction of the measured copy bandwidth under 'kernels' (the raster is issue-bound: its "
-                    "issue and FP32-pipe figures are in profiles/)"}
+                    "fraction of the measured copy bandwidth under 'kernels'; the raster and the cull pass are "
+                    "issue-bound: 'issue' / kernels[*].ncu give issue-active and FP32 (fma) / ALU pipe utilisation "
+                    "from the committed ncu capture (profiles/kernels_serve_small.md)"}
 
 
 def serve_inputs(n: int):
