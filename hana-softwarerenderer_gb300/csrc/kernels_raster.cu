@@ -84,17 +84,18 @@ __constant__ uint32_t kDivMagic[33] = {0,     65536, 32768, 21846, 16384, 13108,
                                        5958,  5462,  5042,  4682,  4370,  4096,  3856,  3641, 3450, 3277, 3121,
                                        2979,  2850,  2731,  2622,  2521,  2428,  2341,  2260, 2185, 2115, 2048};
 
-// The non-empty records of one batch of a tile list, compacted, one array per field: lanes
-// that read different records then hit different shared-memory banks (a 64-byte record per
-// slot would put every even record's field in one bank).
-struct BatchRecs {
-  float ax[32], ay[32], e1x[32], e1y[32], e2x[32], e2y[32], uz[32], d0[32], d1[32], d2[32];
+// The non-empty records of one batch of a tile list, compacted.  The coverage constants a
+// candidate reads are two arrays of float4 and one of uint2 (three shared loads per candidate;
+// consecutive records are consecutive 16-byte entries, so a quarter-warp's loads of different
+// records fall in different banks); the fields resolve reads are one array each.
+struct __align__(16) BatchRecs {
+  float4 a4[32];       // ax, ay, e1x, e1y
+  float4 b4[32];       // e2x, e2y, uz, box (x0 | y0 << 8 | width << 16, bit 31 = kRecExact)
+  uint2 c2[32];        // first candidate of the record's run, ceil(65536 / width)
+  float d0[32], d1[32], d2[32];
   uint32_t seq[32];    // submission order
   uint32_t idx[32];    // record index
   uint32_t pay[32];    // payload index (kept with the winner's weights, in shared memory or the stash)
-  uint32_t off[32];    // first candidate of the record's run
-  uint32_t box[32];    // box in the tile: x0 | y0 << 8 | width << 16, bit 31 = kRecExact
-  uint32_t magic[32];  // ceil(65536 / width): row of a candidate by multiply-shift
 };
 
 // Covered candidates waiting for their weights, depth and visibility update (a ring of 64 per
@@ -320,15 +321,14 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
         __syncwarp();
         if (c > 0u) {  // compact the non-empty runs
           const int k = __popc(ne & ((1u << lane) - 1u));
-          br.ax[k] = rr.ax; br.ay[k] = rr.ay; br.e1x[k] = rr.e1x; br.e1y[k] = rr.e1y;
-          br.e2x[k] = rr.e2x; br.e2y[k] = rr.e2y; br.uz[k] = rr.uz;
+          const uint32_t bits = box | (((rr.view >> kRecFlagShift) & kRecExact) ? 0x80000000u : 0u);
+          br.a4[k] = make_float4(rr.ax, rr.ay, rr.e1x, rr.e1y);
+          br.b4[k] = make_float4(rr.e2x, rr.e2y, rr.uz, __uint_as_float(bits));
+          br.c2[k] = make_uint2(start, kDivMagic[box >> 16]);
           br.d0[k] = rr.d0; br.d1[k] = rr.d1; br.d2[k] = rr.d2;
           br.seq[k] = rr.seq;
           br.idx[k] = ri;
           br.pay[k] = rr.pad;
-          br.off[k] = start;
-          br.box[k] = box | (((rr.view >> kRecFlagShift) & kRecExact) ? 0x80000000u : 0u);
-          br.magic[k] = kDivMagic[box >> 16];
         }
         __syncwarp();
         // Visibility of `cnt` queued candidates from the ring head, one per lane: weights
@@ -345,7 +345,7 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
             const uint32_t jp = cq.jp[e];
             j = (int)(jp & 31u);
             p = (int)(jp >> 8);
-            cover_weights(cq.ux[e], cq.uy[e], br.uz[j], b0, b1, b2);
+            cover_weights(cq.ux[e], cq.uy[e], br.b4[j].z, b0, b1, b2);
             // interpolate_depth (graphics.cpp:186-194)
             const float z = fa(fa(fa(0.f, fm(br.d2[j], b2)), fm(br.d1[j], b1)), fm(br.d0[j], b0));
             key = ((unsigned long long)ord_bits(z) << 32) | (unsigned long long)(0xfffffffeu - br.seq[j]);
@@ -384,15 +384,17 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
           if (i < W) {
             // owner: the last run starting at or before candidate i
             j = (int)(before + (uint32_t)__popc(here & ((2u << lane) - 1u))) - 1;
-            const uint32_t q = i - br.off[j];
-            const uint32_t bx = br.box[j];
+            const float4 a4 = br.a4[j], b4 = br.b4[j];
+            const uint2 c2 = br.c2[j];
+            const uint32_t q = i - c2.x;
+            const uint32_t bx = __float_as_uint(b4.w);
             const uint32_t lw = (bx >> 16) & 255u;
-            const uint32_t qy = (q * br.magic[j]) >> 16;
+            const uint32_t qy = (q * c2.y) >> 16;
             const int lx = (int)(bx & 255u) + (int)(q - qy * lw);
             const int ly = (int)((bx >> 8) & 255u) + (int)qy;
             p = ly * T + lx;
-            covered = cover_terms(br.ax[j], br.ay[j], br.e1x[j], br.e1y[j], br.e2x[j], br.e2y[j], br.uz[j],
-                                  (bx >> 31) != 0u, (float)(ox + lx), (float)(oy + ly), ux, uy);
+            covered = cover_terms(a4.x, a4.y, a4.z, a4.w, b4.x, b4.y, b4.z, (bx >> 31) != 0u, (float)(ox + lx),
+                                  (float)(oy + ly), ux, uy);
           }
           const unsigned cm = __ballot_sync(kFull, covered);
           if (covered) {  // queue behind the pending ones (at most 31 are pending here)
