@@ -92,18 +92,16 @@ struct __align__(16) BatchRecs {
   float4 a4[32];       // ax, ay, e1x, e1y
   float4 b4[32];       // e2x, e2y, uz, box (x0 | y0 << 8 | width << 16, bit 31 = kRecExact)
   uint2 c2[32];        // first candidate of the record's run, ceil(65536 / width)
-  float d0[32], d1[32], d2[32];
-  uint32_t seq[32];    // submission order
-  uint32_t idx[32];    // record index
-  uint32_t pay[32];    // payload index (kept with the winner's weights, in shared memory or the stash)
+  float4 d4[32];       // screen depths d0, d1, d2 of the corners, submission order (bits)
+  uint2 ip[32];        // record index, payload index
 };
 
 // Covered candidates waiting for their weights, depth and visibility update (a ring of 64 per
-// warp): the cross products u.x, u.y of barycentric() and the run | pixel << 8.  The
+// warp): the cross products (u.x, u.y) of barycentric() and the run | pixel << 8.  The
 // coverage pass fills it at the rate candidates are tested; the weights' three divisions and
 // the depth test then run on full warps of covered candidates.
 struct CandQueue {
-  float ux[64], uy[64];
+  float2 u[64];
   uint32_t jp[64];
 };
 
@@ -162,10 +160,9 @@ __device__ __forceinline__ uint32_t shade_tile(const DView& v, const Scratch& sc
         seq = st.seq[p];
       } else if (stash) {
         constexpr int N = T * T;
-        b0 = __ldcg(stash + p);
-        b1 = __ldcg(stash + N + p);
-        b2 = __ldcg(stash + 2 * N + p);
-        pay = __ldcg(reinterpret_cast<const uint32_t*>(stash) + 3 * N + p);
+        const float4 w = __ldcg(reinterpret_cast<const float4*>(stash) + p);
+        b0 = w.x; b1 = w.y; b2 = w.z;
+        pay = __float_as_uint(w.w);
         seq = __ldcg(reinterpret_cast<const uint32_t*>(stash) + 4 * N + p);
       } else {
         const RasterRec r = sc.recs[ri];
@@ -283,14 +280,23 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
     const bool clear = (v.flags & HSR_DRAW_CLEAR) != 0u;
 
     if (n != 0) {  // always: the list holds the tiles with records
+      if (clear) {  // every pixel starts from the clear depth
+        const unsigned long long k0 = buffer_key(v.clear_depth);
 #pragma unroll 8
-      for (int q = 0; q < PPL; q++) {
-        const int p = lane + 32 * q;
-        const int x = ox + p % T, y = oy + p / T;
-        float d = v.clear_depth;
-        if (!clear && x < v.W && y < v.H) d = __ldcg(&v.depth[(size_t)y * v.W + x]);
-        st.key[p] = buffer_key(d);
-        st.rec[p] = kNone;
+        for (int q = 0; q < PPL; q++) {
+          st.key[lane + 32 * q] = k0;
+          st.rec[lane + 32 * q] = kNone;
+        }
+      } else {
+#pragma unroll 8
+        for (int q = 0; q < PPL; q++) {
+          const int p = lane + 32 * q;
+          const int x = ox + p % T, y = oy + p / T;
+          float d = v.clear_depth;
+          if (x < v.W && y < v.H) d = __ldcg(&v.depth[(size_t)y * v.W + x]);
+          st.key[p] = buffer_key(d);
+          st.rec[p] = kNone;
+        }
       }
       uint32_t frags = 0;  // covered candidates of this lane
       for (uint32_t b = 0; b < n; b += 32) {
@@ -325,10 +331,8 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
           br.a4[k] = make_float4(rr.ax, rr.ay, rr.e1x, rr.e1y);
           br.b4[k] = make_float4(rr.e2x, rr.e2y, rr.uz, __uint_as_float(bits));
           br.c2[k] = make_uint2(start, kDivMagic[box >> 16]);
-          br.d0[k] = rr.d0; br.d1[k] = rr.d1; br.d2[k] = rr.d2;
-          br.seq[k] = rr.seq;
-          br.idx[k] = ri;
-          br.pay[k] = rr.pad;
+          br.d4[k] = make_float4(rr.d0, rr.d1, rr.d2, __uint_as_float(rr.seq));
+          br.ip[k] = make_uint2(ri, rr.pad);
         }
         __syncwarp();
         // Visibility of `cnt` queued candidates from the ring head, one per lane: weights
@@ -345,27 +349,28 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
             const uint32_t jp = cq.jp[e];
             j = (int)(jp & 31u);
             p = (int)(jp >> 8);
-            cover_weights(cq.ux[e], cq.uy[e], br.b4[j].z, b0, b1, b2);
+            const float2 u = cq.u[e];
+            const float4 d4 = br.d4[j];
+            cover_weights(u.x, u.y, br.b4[j].z, b0, b1, b2);
             // interpolate_depth (graphics.cpp:186-194)
-            const float z = fa(fa(fa(0.f, fm(br.d2[j], b2)), fm(br.d1[j], b1)), fm(br.d0[j], b0));
-            key = ((unsigned long long)ord_bits(z) << 32) | (unsigned long long)(0xfffffffeu - br.seq[j]);
+            const float z = fa(fa(fa(0.f, fm(d4.z, b2)), fm(d4.y, b1)), fm(d4.x, b0));
+            key = ((unsigned long long)ord_bits(z) << 32) | (unsigned long long)(0xfffffffeu - __float_as_uint(d4.w));
             old = atomicMin(&st.key[p], key);
           }
           __syncwarp();
           if (act && old > key && st.key[p] == key) {
-            st.rec[p] = br.idx[j];
+            const uint2 ip = br.ip[j];
+            const uint32_t seqj = (uint32_t)(0xfffffffeu - (uint32_t)(key & 0xffffffffull));
+            st.rec[p] = ip.x;
             if constexpr (TileState<NPIX>::kKeep) {
-              st.pay[p] = br.pay[j];
-              st.seq[p] = br.seq[j];
+              st.pay[p] = ip.y;
+              st.seq[p] = seqj;
               st.b0[p] = b0;
               st.b1[p] = b1;
               st.b2[p] = b2;
             } else if (stash) {
-              __stcg(stash + p, b0);
-              __stcg(stash + NPIX + p, b1);
-              __stcg(stash + 2 * NPIX + p, b2);
-              __stcg(reinterpret_cast<uint32_t*>(stash) + 3 * NPIX + p, br.pay[j]);
-              __stcg(reinterpret_cast<uint32_t*>(stash) + 4 * NPIX + p, br.seq[j]);
+              __stcg(reinterpret_cast<float4*>(stash) + p, make_float4(b0, b1, b2, __uint_as_float(ip.y)));
+              __stcg(reinterpret_cast<uint32_t*>(stash) + 4 * NPIX + p, seqj);
             }
           }
           qh = (qh + cnt) & 63u;
@@ -400,8 +405,7 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* 
           if (covered) {  // queue behind the pending ones (at most 31 are pending here)
             frags++;
             const uint32_t e = (qh + qn + (uint32_t)__popc(cm & ((1u << lane) - 1u))) & 63u;
-            cq.ux[e] = ux;
-            cq.uy[e] = uy;
+            cq.u[e] = make_float2(ux, uy);
             cq.jp[e] = (uint32_t)j | ((uint32_t)p << 8);
           }
           qn += (uint32_t)__popc(cm);
