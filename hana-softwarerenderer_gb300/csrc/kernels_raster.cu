@@ -204,8 +204,10 @@ __device__ __forceinline__ uint32_t shade_tile(const DView& v, const Scratch& sc
 // The lane whose key is still the minimum after the warp's atomics records the winner's
 // record (two lanes of one step never hold the same key: one triangle covers a pixel
 // once).  Shading then runs once per pixel with a winner.
+// Four-warp CTAs are compiled for 7 per SM (72 registers a thread, fewer spills than at 8 per
+// SM's 64: measured faster on the serving batches, 1.72 -> 1.65 ms).
 template <int T, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster(const DView* __restrict__ views, Scratch sc) {
+__global__ void __launch_bounds__(WARPS * 32, WARPS == 4 ? 7 : 32 / WARPS) k_raster(const DView* __restrict__ views, Scratch sc) {
   constexpr int NPIX = T * T;
   constexpr int PPL = NPIX / 32;
   extern __shared__ __align__(16) unsigned char raster_smem[];
