@@ -718,7 +718,7 @@ constexpr int kPostThreads = 256;
 // Drains the clip queue of k_setup, two faces per warp.  Face pairs are claimed one ahead, so
 // the claim's round trip overlaps the current pair; the grid fills every SM (the queue is short
 // and each face is a chain of dependent loads, so resident warps set the throughput).
-__global__ void __launch_bounds__(kPostThreads, 4) k_post(const DView* __restrict__ views, int T, Scratch sc) {
+__global__ void __launch_bounds__(kPostThreads, 3) k_post(const DView* __restrict__ views, int T, Scratch sc) {
   __shared__ float poly[kPostThreads / 32][2][2][16 * kPolyStride];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, half = lane >> 4;
   if (sc.ctl->error & kErrCapacity) return;
