@@ -219,8 +219,9 @@ int launch_vertex(const DView* views, int nviews, int nchunks, int grid, cudaStr
 constexpr int kSetupCoverPixels = 12;  // pixel ranges up to this size are tested in setup
 
 __device__ __forceinline__ bool coord_ok(float c) {
-  float a = fabsf(c);
-  return (a == 0.f) || (a >= 0x1p-8f && a <= 0x1p20f);
+  // |c| == 0 or 2^-8 <= |c| <= 2^20, on the bits of |c| (NaN and inf are above the range)
+  const uint32_t b = __float_as_uint(c) & 0x7fffffffu;
+  return b == 0u || b - 0x3b800000u <= 0x49800000u - 0x3b800000u;
 }
 
 // Perspective divide of rasterize_triangle (graphics.cpp:321-323): clip / w per component.
@@ -239,15 +240,25 @@ __device__ __forceinline__ bool build_rec(const DView& v, F3 n0, F3 n1, F3 n2, u
   if (sa <= 0.f) return false;
   const F3 s0 = viewport(v.W, v.H, n0), s1 = viewport(v.W, v.H, n1), s2 = viewport(v.W, v.H, n2);
   // bounding box with std::min / std::max (:339-347)
-  float bminx = FLT_MAX, bminy = FLT_MAX, bmaxx = -FLT_MAX, bmaxy = -FLT_MAX;
+  float bminx, bminy, bmaxx, bmaxy;
   const float clampx = (float)(v.W - 1), clampy = (float)(v.H - 1);
   const float sx[3] = {s0.x, s1.x, s2.x}, sy[3] = {s0.y, s1.y, s2.y};
+  if (!(sx[0] != sx[0] || sx[1] != sx[1] || sx[2] != sx[2] || sy[0] != sy[0] || sy[1] != sy[1] || sy[2] != sy[2])) {
+    // no NaN: the chains below reduce to min / max (a signed zero only reaches the (int)
+    // conversions and the < 0 tests, which treat -0 and +0 alike)
+    bminx = fmaxf(0.f, fminf(fminf(sx[0], sx[1]), sx[2]));
+    bmaxx = fminf(clampx, fmaxf(fmaxf(sx[0], sx[1]), sx[2]));
+    bminy = fmaxf(0.f, fminf(fminf(sy[0], sy[1]), sy[2]));
+    bmaxy = fminf(clampy, fmaxf(fmaxf(sy[0], sy[1]), sy[2]));
+  } else {
+    bminx = FLT_MAX; bminy = FLT_MAX; bmaxx = -FLT_MAX; bmaxy = -FLT_MAX;
 #pragma unroll
-  for (int i = 0; i < 3; i++) {
-    bminx = std_max(0.f, std_min(bminx, sx[i]));
-    bmaxx = std_min(clampx, std_max(bmaxx, sx[i]));
-    bminy = std_max(0.f, std_min(bminy, sy[i]));
-    bmaxy = std_min(clampy, std_max(bmaxy, sy[i]));
+    for (int i = 0; i < 3; i++) {
+      bminx = std_max(0.f, std_min(bminx, sx[i]));
+      bmaxx = std_min(clampx, std_max(bmaxx, sx[i]));
+      bminy = std_max(0.f, std_min(bminy, sy[i]));
+      bmaxy = std_min(clampy, std_max(bmaxy, sy[i]));
+    }
   }
   // pixels visited: x from (int)bboxmin.x while x <= bboxmax.x (:350-351)
   const int32_t x0 = cvt_i32(bminx), y0 = cvt_i32(bminy);
