@@ -463,10 +463,12 @@ static void rasterize_triangle(const ctx* c, const v2f* v, uint32_t prim) { /* :
   }
 }
 
-/* graphics_draw_triangle (:378-407) */
-int hsro_draw(const hsro_mesh* mesh, int32_t shader, const hsr_shader_data* sd,
-              const hsro_texture* diffuse, const hsro_texture* normal,
-              const hsro_target* shadow_map, hsro_target* target, uint32_t prim_base) {
+/* graphics_draw_triangle (:378-407); renormalise = Model::normal's in-place normalisation
+ * on every access, or the normals used as stored (the library's hsr_mesh semantics). */
+static int draw_mesh(const hsro_mesh* mesh, int32_t shader, const hsr_shader_data* sd,
+                     const hsro_texture* diffuse, const hsro_texture* normal,
+                     const hsro_target* shadow_map, hsro_target* target, uint32_t prim_base,
+                     int renormalise) {
   if (shader < 0 || shader >= HSR_SHADER_COUNT) return -1;
   ctx c;
   c.sd = sd;
@@ -487,8 +489,10 @@ int hsro_draw(const hsro_mesh* mesh, int32_t shader, const hsr_shader_data* sd,
       const float* uv = &mesh->uv[(size_t)corner[1] * 2];
       float* np = &mesh->nrm[(size_t)corner[2] * 3];
       v3 n = {np[0], np[1], np[2]};
-      n = normalize3(n); /* Model::normal normalises in place (model.cpp:108-111) */
-      np[0] = n.x; np[1] = n.y; np[2] = n.z;
+      if (renormalise) {
+        n = normalize3(n); /* Model::normal normalises in place (model.cpp:108-111) */
+        np[0] = n.x; np[1] = n.y; np[2] = n.z;
+      }
       tri[j] = vertex(&c, p, n, uv);
     }
     int nv = clip_triangle(tri, poly);
@@ -498,6 +502,18 @@ int hsro_draw(const hsro_mesh* mesh, int32_t shader, const hsr_shader_data* sd,
     }
   }
   return 0;
+}
+
+int hsro_draw(const hsro_mesh* mesh, int32_t shader, const hsr_shader_data* sd,
+              const hsro_texture* diffuse, const hsro_texture* normal,
+              const hsro_target* shadow_map, hsro_target* target, uint32_t prim_base) {
+  return draw_mesh(mesh, shader, sd, diffuse, normal, shadow_map, target, prim_base, 1);
+}
+
+int hsro_draw_stored_normals(const hsro_mesh* mesh, int32_t shader, const hsr_shader_data* sd,
+                             const hsro_texture* diffuse, const hsro_texture* normal,
+                             const hsro_target* shadow_map, hsro_target* target, uint32_t prim_base) {
+  return draw_mesh(mesh, shader, sd, diffuse, normal, shadow_map, target, prim_base, 0);
 }
 
 void hsro_clear(hsro_target* t, const uint8_t rgba[4], float depth) { /* renderbuffer.cpp:59-75 */

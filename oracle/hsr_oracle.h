@@ -43,6 +43,12 @@ int hsro_draw(const hsro_mesh* mesh, int32_t shader, const hsr_shader_data* sd,
               const hsro_texture* diffuse, const hsro_texture* normal,
               const hsro_target* shadow_map, hsro_target* target, uint32_t prim_base);
 
+/* The same draw with the normals used as stored, never normalised (the library's hsr_mesh
+ * semantics: a caller that reads normals through Model::normal passes what it returned). */
+int hsro_draw_stored_normals(const hsro_mesh* mesh, int32_t shader, const hsr_shader_data* sd,
+                             const hsro_texture* diffuse, const hsro_texture* normal,
+                             const hsro_target* shadow_map, hsro_target* target, uint32_t prim_base);
+
 /* renderbuffer_clear_color / renderbuffer_clear_depth with explicit bytes; prim -> 0. */
 void hsro_clear(hsro_target* t, const uint8_t rgba[4], float depth);
 

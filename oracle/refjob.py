@@ -16,6 +16,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 HARNESS = os.path.join(HERE, "_ref", "ref_harness")
+SHIM_HOST_HARNESS = os.path.join(HERE, "_ref", "ref_harness_shim_host")
 # The reference's source tree (read only): HSR_REFERENCE_DIR, else where it is unpacked on the
 # build host.  Hosts without it (the GPU hosts) use what `build` left in oracle/_ref.
 REF_DIR = os.environ.get("HSR_REFERENCE_DIR", "/root/reference/Hana-SoftwareRenderer")
@@ -90,10 +91,12 @@ def read_out(path: str) -> dict:
     return out
 
 
-def run(frame, shader: int | None = None, obj_mesh=None, workdir: str | None = None, obj_path: str | None = None) -> dict:
+def run(frame, shader: int | None = None, obj_mesh=None, workdir: str | None = None, obj_path: str | None = None,
+        harness: str = HARNESS) -> dict:
     """Render one frame with the reference.  ``obj_mesh`` overrides the mesh written to
     the OBJ (used for the per-face-uv prim-id run); ``obj_path`` draws an existing OBJ file
-    as Model::Model reads it (a bundled asset, with its own normals)."""
+    as Model::Model reads it (a bundled asset, with its own normals); ``harness`` is the
+    binary that draws (SHIM_HOST_HARNESS: the drop-in shim in place of graphics.cpp)."""
     from hsr import scenes  # noqa: WPS433 (harness-side import)
 
     if obj_mesh is None and obj_path is None and (frame.shader if shader is None else shader) == scenes.FLAT:
@@ -107,7 +110,7 @@ def run(frame, shader: int | None = None, obj_mesh=None, workdir: str | None = N
         job = os.path.join(wd, "job.bin")
         out = os.path.join(wd, "out.bin")
         write_job(job, frame, obj, shader)
-        subprocess.run([HARNESS, "draw", job, out], check=True, stderr=subprocess.DEVNULL)
+        subprocess.run([harness, "draw", job, out], check=True, stderr=subprocess.DEVNULL)
         return read_out(out)
     finally:
         if own:
