@@ -406,7 +406,31 @@ void Runtime::record_result(const Plan& p, const Ctl& c) {
   timing.payload_bytes = c.pay_bytes;
 }
 
+// Index of the first draw that clears a target an earlier draw of the batch writes (n if none).
+// Within one launch sequence the fused clears of all views land before any view is rasterised
+// (empty tiles in the scatter grid), so such a clear cannot follow the earlier draw's pixels there.
+int first_reclear(const hsr_draw_desc* d, int n) {
+  for (int i = 1; i < n; i++)
+    if (d[i].flags & HSR_DRAW_CLEAR)
+      for (int j = 0; j < i; j++)
+        if (d[j].target == d[i].target) return i;
+  return n;
+}
+
+// A batch runs as one launch sequence, or as several in array order where a draw clears a
+// target that an earlier draw of the batch writes (the sequential semantics of the calls).
 int Runtime::run_batch(const hsr_draw_desc* descs, int n) {
+  while (n > 0) {
+    const int k = first_reclear(descs, n);
+    const int rc = run_sequence(descs, k);
+    if (rc != HSR_OK) return rc;
+    descs += k;
+    n -= k;
+  }
+  return HSR_OK;
+}
+
+int Runtime::run_sequence(const hsr_draw_desc* descs, int n) {
   if (n <= 0) return HSR_OK;
   Plan p;
   int rc = plan_build(descs, n, p);

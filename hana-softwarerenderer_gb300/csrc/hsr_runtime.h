@@ -80,6 +80,10 @@ struct Plan {
   bool grow(const Ctl& c);
 };
 
+// Index of the first draw that clears a target an earlier draw of the batch writes (n if none):
+// a batch runs as one launch sequence up to there.
+int first_reclear(const hsr_draw_desc* d, int n);
+
 struct Runtime {
   int device = 0;
   int num_sms = 1;
@@ -112,7 +116,8 @@ struct Runtime {
   // A plan overflowed and grew: later plans start from at least its capacities (every path
   // that launches plans, so one overflow is not repeated by each later batch).
   void learn_caps(const Plan& p);
-  int run_batch(const hsr_draw_desc* descs, int n);
+  int run_batch(const hsr_draw_desc* descs, int n);     // one or more launch sequences
+  int run_sequence(const hsr_draw_desc* descs, int n);  // one launch sequence
   int clear_target(TargetObj* t, const uint8_t rgba[4], float depth);
 
  private:

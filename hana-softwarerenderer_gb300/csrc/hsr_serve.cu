@@ -475,6 +475,9 @@ extern "C" {
 int hsr_plan_create(const hsr_draw_desc* descs, int32_t n, hsr_plan* out) {
   RT_LOCK();
   if (!descs || n <= 0 || !out) return fail(HSR_ERR_INVALID_ARG, "plan_create: bad arguments");
+  if (first_reclear(descs, n) < n)
+    return fail(HSR_ERR_INVALID_ARG, "plan_create: a draw clears a target an earlier draw of the plan writes "
+                                     "(one plan is one launch sequence: make two plans)");
   PlanObj* po = new PlanObj();
   po->descs.assign(descs, descs + n);
   po->uniforms.resize(n);

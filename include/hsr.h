@@ -220,7 +220,9 @@ HSR_API int hsr_target_write_tga(hsr_target t, const char* path, int32_t rle);
  * hsr_draw: one graphics_draw_triangle() call, queued on the library stream.
  * hsr_draw_batch: n draws in one launch sequence.  A draw whose shadow_map is the target
  * of another draw in the batch runs after it (the DrawModel::draw order, scene.h:86-91);
- * several draws into one target keep their array order. */
+ * several draws into one target keep their array order.  A draw with HSR_DRAW_CLEAR into a
+ * target that an earlier draw of the batch writes starts a new launch sequence, so that its
+ * clear follows that draw as it would with separate calls. */
 HSR_API int hsr_draw(const hsr_draw_desc* desc);
 HSR_API int hsr_draw_batch(const hsr_draw_desc* descs, int32_t n);
 HSR_API int hsr_synchronize(void);
@@ -287,9 +289,10 @@ typedef struct hsr_stats {
 HSR_API int hsr_get_stats(hsr_stats* out);
 
 /* ---- plans: a batch recorded once into a CUDA graph and replayed ------------------------
- * hsr_plan_create validates the draws (same rules as hsr_draw_batch), reserves the plan's own
- * scratch, and records the whole launch sequence (descriptor upload, counter reset, seven
- * kernels) into a CUDA graph.  Between replays only uniforms may change
+ * hsr_plan_create validates the draws (same rules as hsr_draw_batch; a plan is one launch
+ * sequence, so a draw that clears a target an earlier draw of the plan writes is refused with
+ * HSR_ERR_INVALID_ARG), reserves the plan's own scratch, and records the whole launch sequence
+ * (descriptor upload, counter reset, eight kernels) into a CUDA graph.  Between replays only uniforms may change
  * (hsr_plan_set_uniforms); meshes, textures, targets and shaders stay those of creation.
  * hsr_plan_launch replays the graph on the library stream and returns at once;
  * hsr_plan_wait blocks until it is done and re-runs it with larger scratch if the device

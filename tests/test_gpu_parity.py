@@ -141,6 +141,44 @@ def test_multi_draw_same_target(gpu):
     assert_parity({"main": got2}, exp, "multi-draw calls")
 
 
+def test_a_second_clear_of_a_target_follows_the_earlier_draws(gpu):
+    """[A clear, B clear, C] into one target, as one batch and as three calls, equals the
+    reference's sequence: B's clear erases A, then B and C draw (C tests against B's depth).
+    The batch runs as two launch sequences, split before B; a plan (one launch sequence)
+    refuses it."""
+    import hsr
+
+    fa = scenes.sphere_frame(3, 160, 120, shader=scenes.BLINN, eye=(0.2, 0.1, 2.4), tex_size=64, seed=2)
+    fb = scenes.displaced_frame(3, 160, 120, shadow=0, tex_size=64, shader=scenes.TEXTURE, eye=(0.5, 0.3, 2.2))
+    fc = scenes.sphere_frame(3, 160, 120, shader=scenes.TOON, eye=(-0.4, 0.2, 2.0), tex_size=64, seed=7)
+    b_clear = ((10, 20, 30, 40), 100.0)
+    tgt = hsr.Target(160, 120)
+    ma, mb, mc = hsr.Mesh(fa.mesh), hsr.Mesh(fb.mesh), hsr.Mesh(fc.mesh)
+    ta, tb, tc = hsr.Texture(fa.diffuse), hsr.Texture(fb.diffuse), hsr.Texture(fc.diffuse)
+    keep = []
+    try:
+        d1 = hsr.make_desc(ma, fa.shader, fa.sd, tgt, ta, clear=(fa.clear_rgba, fa.clear_depth), keep=keep)
+        d2 = hsr.make_desc(mb, fb.shader, fb.sd, tgt, tb, clear=b_clear, prim_base=1_000_000, keep=keep)
+        d3 = hsr.make_desc(mc, fc.shader, fc.sd, tgt, tc, prim_base=2_000_000, keep=keep)
+        hsr.draw_batch([d1, d2, d3])
+        got = tgt.download()
+        for d in (d1, d2, d3):
+            hsr.draw(d)
+        got2 = tgt.download()
+        with pytest.raises(gpu.HsrError) as e:
+            hsr.Plan([d1, d2, d3])
+        assert e.value.code == gpu.ERR_INVALID_ARG
+    finally:
+        for o in (tgt, ma, mb, mc, ta, tb, tc):
+            o.release()
+    rb = oracle.Buffers(160, 120, *b_clear)
+    oracle.draw(fb.mesh, fb.shader, fb.sd, rb, fb.diffuse, prim_base=1_000_000)
+    oracle.draw(fc.mesh, fc.shader, fc.sd, rb, fc.diffuse, prim_base=2_000_000)
+    exp = {"main": {"depth": rb.depth, "color": rb.color, "prim": rb.prim}}
+    assert_parity({"main": got}, exp, "re-clear batch")
+    assert_parity({"main": got2}, exp, "re-clear calls")
+
+
 def test_draw_without_clear_keeps_untouched_pixels(gpu):
     import hsr
 
