@@ -169,9 +169,9 @@ def kernel_bytes(t: dict) -> dict:
              once) + a 64 B record written per triangle that reaches the raster.
     emit   : per surviving triangle 32 B of its record and 16 B face indices read, a 4 B
              payload index written, and the shading payload written (payload_bytes, counted
-             by the kernels: 0-128 B by shader); the position, normal, uv and screen vertex
-             (56 B) of each vertex of a surviving triangle read once, records / 2 vertices
-             (a closed triangle mesh has half as many vertices as faces).
+             by the kernels: 0-128 B by shader); the packed position, normal and uv (one
+             32 B sector) of each vertex of a surviving triangle read once, records / 2
+             vertices (a closed triangle mesh has half as many vertices as faces).
     clip   : per clipped face 48 B of indices and 3 x 56 B of corner attributes.
     split  : per split triangle its 192 B queue entry read.
     scan   : 4 B read + 12 B written per tile (offset, non-empty prefix, list entry).
@@ -188,7 +188,7 @@ def kernel_bytes(t: dict) -> dict:
     return {
         "vertex": t["vertices"] * 28 + t["normals"] * 28,
         "cull": t["faces"] * 16 + t["vertices"] * 16 + rec * 64,
-        "emit": rec * 52 + pay + (rec // 2) * 56,
+        "emit": rec * 52 + pay + (rec // 2) * 32,
         "clip": t["clipped_faces"] * (48 + 3 * 56),
         "split": t.get("split_triangles", 0) * 192,
         "scan": t.get("tiles", px / 64.0) * 16,

@@ -195,10 +195,10 @@ struct Scratch {
   uint32_t faults;          // HSR_FAULT_* injected by the host (tests of the failure paths)
   int32_t poll_limit;       // polls before a bounded wait gives up (0: the defaults above)
 };
-// Per raster warp of a 16x16 or 32x32 tile, per pixel: the winner's weights b0, b1, b2 and
-// payload index as one 16-byte entry, then (after all of those) its submission word — what
-// shading would otherwise re-derive from the record.
-__host__ __device__ constexpr int stash_floats(int tile) { return 5 * tile * tile; }
+// Per raster warp of a 16x16 or 32x32 tile, per pixel: the winner's weights b0, b1, b2 as one
+// 16-byte entry — what shading would otherwise re-derive from the record.  (The winner's record
+// index, which is also its payload index, and its submission word are in the tile's shared state.)
+__host__ __device__ constexpr int stash_floats(int tile) { return 4 * tile * tile; }
 constexpr int kStashWarpsPerSm = 32;  // raster warps resident per SM at most
 
 // Kernel launchers (kernels_*.cu).  All return cudaError_t as int.

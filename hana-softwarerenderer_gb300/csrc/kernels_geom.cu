@@ -786,10 +786,13 @@ __global__ void __launch_bounds__(kBigThreads) k_big(const DView* __restrict__ v
     __syncthreads();
     const uint32_t base = s_base;
     if ((uint64_t)base + (uint64_t)nsub > (uint64_t)sc.rec_cap) continue;
+    // every sub-record carries its own copy of the payload, so that a record's payload index is
+    // its own index (the raster loads the payload from the record index in shared memory)
     const int nf4 = payload_f4(v.shader);
-    if ((int)threadIdx.x < nf4)
-      reinterpret_cast<float4*>(&sc.pay[base])[threadIdx.x] = reinterpret_cast<const float4*>(&bi.pay)[threadIdx.x];
-    if (threadIdx.x == 0 && nf4) atomicAdd(&sc.ctl->pay_bytes, 16ull * (unsigned long long)nf4);
+    for (int k = threadIdx.x; k < nsub * nf4; k += kBigThreads)
+      reinterpret_cast<float4*>(&sc.pay[base + (uint32_t)(k / nf4)])[k % nf4] =
+          reinterpret_cast<const float4*>(&bi.pay)[k % nf4];
+    if (threadIdx.x == 0 && nf4) atomicAdd(&sc.ctl->pay_bytes, 16ull * (unsigned long long)(nf4 * nsub));
     const int x0 = (int)(b.xr & 0xffffu), x1 = (int)(b.xr >> 16);
     const int y0 = (int)(b.yr & 0xffffu), y1 = (int)(b.yr >> 16);
     for (int sidx = threadIdx.x; sidx < nsub; sidx += kBigThreads) {
@@ -799,7 +802,7 @@ __global__ void __launch_bounds__(kBigThreads) k_big(const DView* __restrict__ v
       RasterRec w = b;
       w.xr = (uint32_t)max(x0, stx0 * T) | ((uint32_t)min(x1, stx1 * T + T - 1) << 16);
       w.yr = (uint32_t)max(y0, sty0 * T) | ((uint32_t)min(y1, sty1 * T + T - 1) << 16);
-      w.pad = base;
+      w.pad = base + (uint32_t)sidx;
       store_rec(&sc.recs[base + (uint32_t)sidx], w);
     }
     for (int k = threadIdx.x; k < nt; k += kBigThreads)

@@ -93,7 +93,7 @@ struct __align__(16) BatchRecs {
   float4 b4[32];       // e2x, e2y, uz, box (x0 | y0 << 8 | width << 16, bit 31 = kRecExact)
   uint2 c2[32];        // first candidate of the record's run, ceil(65536 / width)
   float4 d4[32];       // screen depths d0, d1, d2 of the corners, submission order (bits)
-  uint2 ip[32];        // record index, payload index
+  uint32_t ri[32];     // record index (also the index of its payload)
 };
 
 // Covered candidates waiting for their weights, depth and visibility update (a ring of 64 per
@@ -106,16 +106,14 @@ struct CandQueue {
 };
 
 // Per-warp tile state in shared memory: per pixel the key (ordered depth | submission) and
-// the index of the record that holds it.  8x8 tiles also keep the winner's payload index,
-// submission number and barycentric weights (28 bytes a pixel), so shading reads no record;
-// 16x16 tiles keep 12 bytes a pixel, which leaves room for 8 warps of them per SM, and
-// shading evaluates the weights again from the record.
+// the index of the record that holds it, which is also the index of its payload.  8x8 tiles
+// also keep the winner's barycentric weights (24 bytes a pixel in all), so shading reads no
+// record; 16x16 and 32x32 tiles keep 12 bytes a pixel and the weights in the warp's stash.
 template <int NPIX>
 struct TileState {
   static constexpr bool kKeep = NPIX <= 64;
   unsigned long long key[NPIX];
   uint32_t rec[NPIX];
-  uint32_t pay[kKeep ? NPIX : 1], seq[kKeep ? NPIX : 1];
   float b0[kKeep ? NPIX : 1], b1[kKeep ? NPIX : 1], b2[kKeep ? NPIX : 1];
 };
 
@@ -154,16 +152,17 @@ __device__ __forceinline__ uint32_t shade_tile(const DView& v, const Scratch& sc
       shaded++;
       float b0, b1, b2;
       uint32_t pay, seq;
+      // a record's payload index is its own index, and the winner's submission is the low word of
+      // its key: the payload's loads wait for nothing but the record index
       if constexpr (TileState<T * T>::kKeep) {
         b0 = st.b0[p]; b1 = st.b1[p]; b2 = st.b2[p];
-        pay = st.pay[p];
-        seq = st.seq[p];
+        pay = ri;
+        seq = 0xfffffffeu - (uint32_t)st.key[p];
       } else if (stash) {
-        constexpr int N = T * T;
+        pay = ri;
+        seq = 0xfffffffeu - (uint32_t)st.key[p];
         const float4 w = __ldcg(reinterpret_cast<const float4*>(stash) + p);
         b0 = w.x; b1 = w.y; b2 = w.z;
-        pay = __float_as_uint(w.w);
-        seq = __ldcg(reinterpret_cast<const uint32_t*>(stash) + 4 * N + p);
       } else {
         const RasterRec r = sc.recs[ri];
         cover_test(r.ax, r.ay, r.e1x, r.e1y, r.e2x, r.e2y, r.uz, ((r.view >> kRecFlagShift) & kRecExact) != 0u,
@@ -334,7 +333,7 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 4 ? 7 : 32 / WARPS) k_ras
           br.b4[k] = make_float4(rr.e2x, rr.e2y, rr.uz, __uint_as_float(bits));
           br.c2[k] = make_uint2(start, kDivMagic[box >> 16]);
           br.d4[k] = make_float4(rr.d0, rr.d1, rr.d2, __uint_as_float(rr.seq));
-          br.ip[k] = make_uint2(ri, rr.pad);
+          br.ri[k] = ri;
         }
         __syncwarp();
         // Visibility of `cnt` queued candidates from the ring head, one per lane: weights
@@ -361,18 +360,13 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 4 ? 7 : 32 / WARPS) k_ras
           }
           __syncwarp();
           if (act && old > key && st.key[p] == key) {
-            const uint2 ip = br.ip[j];
-            const uint32_t seqj = (uint32_t)(0xfffffffeu - (uint32_t)(key & 0xffffffffull));
-            st.rec[p] = ip.x;
+            st.rec[p] = br.ri[j];
             if constexpr (TileState<NPIX>::kKeep) {
-              st.pay[p] = ip.y;
-              st.seq[p] = seqj;
               st.b0[p] = b0;
               st.b1[p] = b1;
               st.b2[p] = b2;
             } else if (stash) {
-              __stcg(reinterpret_cast<float4*>(stash) + p, make_float4(b0, b1, b2, __uint_as_float(ip.y)));
-              __stcg(reinterpret_cast<uint32_t*>(stash) + 4 * NPIX + p, seqj);
+              __stcg(reinterpret_cast<float4*>(stash) + p, make_float4(b0, b1, b2, 0.f));
             }
           }
           qh = (qh + cnt) & 63u;
