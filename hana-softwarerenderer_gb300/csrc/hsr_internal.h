@@ -53,7 +53,7 @@ enum : uint32_t {
                    // exact: the raster evaluates the reference's divisions instead
   kRecHole = 2u,   // slot of a huge triangle handed to k_big: binned nowhere
 };
-constexpr uint32_t kPadPending = 0xffffffffu;  // RasterRec::pad of a record k_emit has not finished
+constexpr uint32_t kPadPending = 0xffffffffu;  // RasterRec::pad of the cull pass's records: the ones k_emit completes
 
 // One triangle that reached the raster (64 bytes).  A, B-A, C-A are the per-triangle
 // constants of barycentric() (graphics.cpp:222-233); uz is u.z, constant per triangle.
@@ -65,7 +65,8 @@ struct __align__(16) RasterRec {
   uint32_t view;            // index of the view in the batch | flags << 28 (kRec*)
   uint32_t xr, yr;          // inclusive pixel range: x0 | x1 << 16, y0 | y1 << 16
   uint32_t rsv;             // reserved (zero)
-  uint32_t pad;             // payload index
+  uint32_t pad;             // kPadPending on the cull pass's records (the emit pass's work), else 0;
+                            // a record's payload is at the record's own index
 };
 constexpr uint32_t kRecViewMask = 0x0fffffffu;
 constexpr int kRecFlagShift = 28;

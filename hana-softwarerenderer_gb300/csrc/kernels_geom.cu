@@ -394,14 +394,14 @@ __device__ __forceinline__ uint32_t block_reserve(bool want, uint32_t* counter) 
 // Store the records of a warp at their slots (at most one per lane, each touching
 // <= kMaxRecordTiles tiles) with their payloads, and count the tiles they touch,
 // aggregating equal tiles across lanes.  All 32 lanes call this.
-// With `only_pad`, the record is already in place and only its payload index is written.
+// With `in_place`, the record is already stored (the emit pass): only its payload (at the
+// record's own index) and its tile counts are written.
 __device__ void append_counts(bool valid, uint32_t slot, const RasterRec& r, const Payload& pl, int nf4, const DView& v,
-                              int T, const Scratch& sc, bool only_pad = false) {
+                              int T, const Scratch& sc, bool in_place = false) {
   const int lane = threadIdx.x & 31;
   int tx0 = 0, ty0 = 0, ntw = 1, nt = 0;
   if (valid) {
-    if (only_pad) sc.recs[slot].pad = r.pad;
-    else store_rec(&sc.recs[slot], r);
+    if (!in_place) store_rec(&sc.recs[slot], r);
     store_payload(&sc.pay[slot], pl, nf4);
     rec_tiles(r, T, tx0, ty0, ntw, nt);
   }
@@ -420,7 +420,6 @@ __device__ void append_small(bool valid, uint32_t slot, RasterRec r, const Paylo
                              int T, const Scratch& sc) {
   const bool ok = valid && slot < sc.rec_cap;
   if (valid && !ok) atomicOr(&sc.ctl->error, kErrRecOverflow);
-  r.pad = slot;  // payload index
   append_counts(ok, slot, r, pl, nf4, v, T, sc);
 }
 
@@ -616,7 +615,6 @@ __global__ void __launch_bounds__(kEmitThreads, 4) k_emit(const DView* __restric
     const bool big = valid && nt > kMaxRecordTiles;
     const bool small = valid && !big;
     if (small) {
-      r.pad = i;  // payload index
       pay_bytes += 16u * (uint32_t)nf4;
     }
     append_counts(small, i, r, pl, nf4, *v, T, sc, true);
@@ -802,7 +800,7 @@ __global__ void __launch_bounds__(kBigThreads) k_big(const DView* __restrict__ v
       RasterRec w = b;
       w.xr = (uint32_t)max(x0, stx0 * T) | ((uint32_t)min(x1, stx1 * T + T - 1) << 16);
       w.yr = (uint32_t)max(y0, sty0 * T) | ((uint32_t)min(y1, sty1 * T + T - 1) << 16);
-      w.pad = base + (uint32_t)sidx;
+      w.pad = 0u;
       store_rec(&sc.recs[base + (uint32_t)sidx], w);
     }
     for (int k = threadIdx.x; k < nt; k += kBigThreads)

@@ -167,7 +167,7 @@ __device__ __forceinline__ uint32_t shade_tile(const DView& v, const Scratch& sc
         const RasterRec r = sc.recs[ri];
         cover_test(r.ax, r.ay, r.e1x, r.e1y, r.e2x, r.e2y, r.uz, ((r.view >> kRecFlagShift) & kRecExact) != 0u,
                    (float)x, (float)y, b0, b1, b2);
-        pay = r.pad;
+        pay = ri;
         seq = r.seq;
       }
       float P[NF4 > 0 ? NF4 * 4 : 4];
