@@ -130,10 +130,10 @@ struct RasterSmem {
 
 // Shade the winners of one tile and write colour, depth and prim id (fused clear writes the
 // clear values where nothing won).  S is the shader, known at compile time.  Without kept
-// weights (16x16 tiles) the winner's weights, payload index and submission come from the
-// warp's stash in global memory (written by the visibility pass, read back from L2), or, with
-// no stash, are evaluated again from its record: the same operations on the same values as in
-// the visibility pass either way, so the same bits.
+// weights (16x16 and 32x32 tiles) the winner's weights come from the warp's stash in global
+// memory (written by the visibility pass, read back from L2), or, with no stash, are evaluated
+// again from its record: the same operations on the same values as in the visibility pass
+// either way, so the same bits.
 template <int T, int S>
 __device__ __forceinline__ uint32_t shade_tile(const DView& v, const Scratch& sc, const TileState<T * T>& st, int ox,
                                                int oy, bool clear, const ByteTables& bt, const float* stash) {
