@@ -53,21 +53,21 @@ enum : uint32_t {
                    // exact: the raster evaluates the reference's divisions instead
   kRecHole = 2u,   // slot of a huge triangle handed to k_big: binned nowhere
 };
-constexpr uint32_t kPadPending = 0xffffffffu;  // RasterRec::pad of the cull pass's records: the ones k_emit completes
 
 // One triangle that reached the raster (64 bytes).  A, B-A, C-A are the per-triangle
-// constants of barycentric() (graphics.cpp:222-233); uz is u.z, constant per triangle.
+// constants of barycentric() (graphics.cpp:222-233); uz is u.z, constant per triangle.  The
+// last 16 bytes are the words the emit pass and the scatter read (one 16-byte load each); a
+// record's payload is at the record's own index.
 struct __align__(16) RasterRec {
   float ax, ay, e1x, e1y;   // A; e1 = B - A
   float e2x, e2y, uz, d0;   // e2 = C - A; u.z; screen depth of A
   float d1, d2;             // screen depths of B, C
+  uint32_t rsv, pad;        // reserved (zero)
   uint32_t seq;             // (face << 4) | (fan << 1) | clipped — submission order
   uint32_t view;            // index of the view in the batch | flags << 28 (kRec*)
   uint32_t xr, yr;          // inclusive pixel range: x0 | x1 << 16, y0 | y1 << 16
-  uint32_t rsv;             // reserved (zero)
-  uint32_t pad;             // kPadPending on the cull pass's records (the emit pass's work), else 0;
-                            // a record's payload is at the record's own index
 };
+static_assert(offsetof(RasterRec, seq) == 48 && offsetof(RasterRec, yr) == 60, "binning words in the last 16 bytes");
 constexpr uint32_t kRecViewMask = 0x0fffffffu;
 constexpr int kRecFlagShift = 28;
 

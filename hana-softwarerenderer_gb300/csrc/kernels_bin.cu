@@ -163,10 +163,12 @@ __device__ __forceinline__ void scatter_records(const DView* __restrict__ views,
     const uint32_t i = i0 + (uint32_t)lane;
     const bool ok = i < nrec;
     int tx0 = 0, ty0 = 0, ntw = 0, nt = 0, tbase = 0, tiles_x = 0;
-    if (ok && !((sc.recs[i].view >> kRecFlagShift) & kRecHole)) {  // holes: huge triangles split by k_big
-      const RasterRec& r = sc.recs[i];
-      const uint32_t xr = r.xr, yr = r.yr;
-      const DView& v = views[r.view & kRecViewMask];
+    // the record's view and pixel range: its last 16 bytes (seq, view, xr, yr) in one load
+    const uint4 w = ok ? *reinterpret_cast<const uint4*>(reinterpret_cast<const char*>(&sc.recs[i]) + 48)
+                       : make_uint4(0u, kRecHole << kRecFlagShift, 0u, 0u);
+    if (ok && !((w.y >> kRecFlagShift) & kRecHole)) {  // holes: huge triangles split by k_big
+      const uint32_t xr = w.z, yr = w.w;
+      const DView& v = views[w.y & kRecViewMask];
       tbase = v.tile_base;
       tiles_x = v.tiles_x;
       tx0 = (int)(xr & 0xffffu) >> ts;

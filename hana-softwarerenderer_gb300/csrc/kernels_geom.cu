@@ -447,7 +447,7 @@ constexpr int kPolyStride = kVaryings;  // floats per polygon vertex in shared m
 
 // Cull pass, one thread per face: fast accept, cull, viewport, bounding box and the
 // coverage check of small ranges; a surviving triangle's 64-byte record is stored at a
-// block-reserved slot (pad = kPadPending: payload and tile counts are still to come), and
+// block-reserved slot (its payload and tile counts are still to come: k_emit), and
 // faces that need the clipper are queued.  Four in five faces of the serving batches die
 // here, so the per-record work runs in k_emit on dense warps instead of on the few lanes
 // that survive in each warp of this pass.
@@ -508,7 +508,6 @@ __global__ void __launch_bounds__(kSetupThreads, 8) k_setup(const DView* __restr
     const uint32_t slot = block_reserve<kSetupThreads>(valid, &sc.ctl->rec_count);
     if (valid) {
       if (slot < sc.rec_cap) {
-        r.pad = kPadPending;
         store_rec(&sc.recs[slot], r);
       } else {
         atomicOr(&sc.ctl->error, kErrRecOverflow);
@@ -595,12 +594,12 @@ __global__ void __launch_bounds__(kEmitThreads, 4) k_emit(const DView* __restric
     int nf4 = 0;
     const DView* v = views;
     if (i < nrec) {
-      // the words this pass needs (seq, view, pixel range, pad); the whole record only
-      // for a huge triangle
-      const uint4 a = *reinterpret_cast<const uint4*>(reinterpret_cast<const char*>(&sc.recs[i]) + 32);
-      const uint4 b = *reinterpret_cast<const uint4*>(reinterpret_cast<const char*>(&sc.recs[i]) + 48);
-      r.seq = a.z; r.view = a.w; r.xr = b.x; r.yr = b.y; r.rsv = b.z; r.pad = b.w;
-      valid = r.pad == kPadPending;  // written by k_setup in this launch sequence
+      // the words this pass needs (seq, view, pixel range: the record's last 16 bytes); the
+      // whole record only for a huge triangle.  Every record below the count is the cull
+      // pass's: the clipper and k_big append theirs after this pass.
+      const uint4 a = *reinterpret_cast<const uint4*>(reinterpret_cast<const char*>(&sc.recs[i]) + 48);
+      r.seq = a.x; r.view = a.y; r.xr = a.z; r.yr = a.w;
+      valid = true;
       if (valid) {
         v = views + (r.view & kRecViewMask);
         nf4 = payload_f4(v->shader);
