@@ -297,6 +297,14 @@ __device__ __forceinline__ Col fragment_s(const DView& v, const float* P, float 
   }
 }
 
+// 32-byte vector global store (sm_100 and later): two float4s in one instruction, so the record
+// and payload stores of the cull and emit passes take half the load/store-unit slots; the address
+// must be 32-byte aligned (records are 64 bytes, payloads 128, both arrays 256-byte aligned).
+__device__ __forceinline__ void st_v8(void* p, float4 a, float4 b) {
+  asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "f"(a.x), "f"(a.y), "f"(a.z), "f"(a.w),
+               "f"(b.x), "f"(b.y), "f"(b.z), "f"(b.w)
+               : "memory");
+}
 // set_color (renderbuffer.cpp:38-44): R, G, B through (uchar)(c*255); alpha kept.
 __device__ __forceinline__ uint32_t pack_rgb(Col c, uint32_t alpha_word) {
   uint32_t r = (uint32_t)cvt_i32(fm(c.r, 255.f)) & 255u;

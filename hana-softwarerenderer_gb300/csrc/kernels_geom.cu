@@ -296,9 +296,9 @@ __device__ __forceinline__ bool build_rec(const DView& v, F3 n0, F3 n1, F3 n2, u
 }
 
 __device__ __forceinline__ void store_rec(RasterRec* dst, const RasterRec& r) {
-  float4* d = reinterpret_cast<float4*>(dst);
   const float4* s = reinterpret_cast<const float4*>(&r);
-  d[0] = s[0]; d[1] = s[1]; d[2] = s[2]; d[3] = s[3];
+  st_v8(dst, s[0], s[1]);
+  st_v8(reinterpret_cast<char*>(dst) + 32, s[2], s[3]);
 }
 
 // Payload floats a shader reads, rounded up to whole float4s (see the Payload layout).
@@ -336,8 +336,10 @@ __device__ __forceinline__ void store_payload(Payload* dst, const Payload& p, in
   float4* d = reinterpret_cast<float4*>(dst);
   const float4* s = reinterpret_cast<const float4*>(&p);
 #pragma unroll
-  for (int q = 0; q < 8; q++)
-    if (q < nf4) d[q] = s[q];
+  for (int q = 0; q < 8; q += 2) {
+    if (q + 1 < nf4) st_v8(d + q, s[q], s[q + 1]);
+    else if (q < nf4) d[q] = s[q];
+  }
 }
 
 // Tile rectangle of a record; T is a power of two (8 or 16).
