@@ -602,13 +602,11 @@ __global__ void __launch_bounds__(kEmitThreads, 4) k_emit(const DView* __restric
       const uint4 a = *reinterpret_cast<const uint4*>(reinterpret_cast<const char*>(&sc.recs[i]) + 48);
       r.seq = a.x; r.view = a.y; r.xr = a.z; r.yr = a.w;
       valid = true;
-      if (valid) {
-        v = views + (r.view & kRecViewMask);
-        nf4 = payload_f4(v->shader);
-        if (nf4 > 0) {
-          const int f = (int)(r.seq >> 4);
-          face_payload(*v, f, nf4, __ldg(&v->fv[f]), pl);
-        }
+      v = views + (r.view & kRecViewMask);
+      nf4 = payload_f4(v->shader);
+      if (nf4 > 0) {
+        const int f = (int)(r.seq >> 4);
+        face_payload(*v, f, nf4, __ldg(&v->fv[f]), pl);
       }
     }
     int tx0, ty0, ntw, nt = 0;
