@@ -398,18 +398,18 @@ def run_ours(args, world, rank, local):
 
 def serve_poisson(rp, reqs, plain_fps: float, server_fps: float, args) -> dict:
     """The 10,000-request Poisson stream at two offered loads, server vs plain path.  One
-    long-running server serves both loads; it is warmed first with 512 requests of the stream at
-    once (untimed), so that its scratch and staging have reached their working size, as they
-    would have in a server that has been running."""
+    long-running server serves both loads; it is warmed first with the whole stream at once
+    (untimed), so that its scratch and staging have reached the working size of this stream's
+    batches, as they would have in a server that has been running."""
     import hsr
     from hsr import scenes
     from hsr import serve as hserve
 
-    res = {"requests": len(reqs), "arrivals": "Poisson", "server_warmup_requests": 512}
+    res = {"requests": len(reqs), "arrivals": "Poisson", "server_warmup_requests": len(reqs)}
     srv = hsr.Server(40 << 30, BATCH, 2)
     ring = hserve.PinnedRing(1 << 30)
     try:
-        hserve.serve_batched(rp, scenes.retime(reqs[:512], 1e9), server=srv, ring=ring)
+        hserve.serve_batched(rp, scenes.retime(reqs, 1e9), server=srv, ring=ring)
         for name, rate in (("load_plain80", 0.8 * plain_fps), ("load_server80", 0.8 * server_fps)):
             stream = scenes.retime(reqs, rate, seed=11)
             b = hserve.serve_batched(rp, stream, server=srv, ring=ring)
