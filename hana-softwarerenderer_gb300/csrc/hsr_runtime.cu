@@ -2,8 +2,10 @@
 //
 // Replaces graphics_draw_triangle(DrawData*) (graphics.h:15, graphics.cpp:378-407) by
 // handle-based calls.  Meshes, textures and targets live in device memory; hsr_draw_batch
-// turns a list of draws into one launch sequence (vertex, setup, scan, scatter, raster)
-// over all of them.  Scratch is a grow-only arena; an overflow detected on the device
+// turns a list of draws into one launch sequence of eight kernels (vertex, cull, emit, clip,
+// split, scan, scatter, raster) over all of them, or into several in array order where a draw
+// clears a target an earlier draw of the list writes.  Scratch is a grow-only arena; an
+// overflow detected on the device
 // leaves the targets untouched (the raster checks the error word first) and the batch is
 // re-run with larger capacity.  No CPU fallback exists: without a device every call
 // fails with a status code.

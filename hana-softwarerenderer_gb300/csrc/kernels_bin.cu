@@ -7,7 +7,7 @@
 //           block order comes from a ticket so a block only waits on blocks that already
 //           run, and every wait is bounded (error bit + give up, never a hang).
 // k_scatter writes record indices into the per-tile lists with warp-aggregated atomics;
-//           a record touches at most kMaxRecordTiles tiles (setup splits larger ones).
+//           a record touches at most kMaxRecordTiles tiles (k_big splits larger ones).
 //           The same grid clears the tiles no record touches, streamed in row order.
 #include "hsr_device.cuh"
 

@@ -13,10 +13,13 @@
 // survives setup: k_emit (and the clipper) transform them per corner (world_pos_of,
 // world_normal_of) instead of this pass writing and re-reading them for every vertex.
 //
-// k_setup follows graphics.cpp:136-161 (clip) and :314-347 (cull, viewport, bounding box)
-// for every fan triangle and emits one RasterRec.  Faces that fail the fast accept are
-// clipped by the whole warp: lane k carries varying k of the polygon through
-// Sutherland-Hodgman while every lane evaluates the plane tests on the clip coordinates.
+// k_setup (the cull pass) follows graphics.cpp:136-161 (clip) and :314-347 (cull, viewport,
+// bounding box) for every face that passes the fast accept and stores one RasterRec per
+// surviving triangle; faces that need the clipper are queued.  k_emit writes the surviving
+// records' shading payloads and tile counts on dense warps; k_post clips the queued faces (two
+// per warp: lane k of a half-warp carries varying k of the polygon through Sutherland-Hodgman)
+// and emits their fan triangles; k_big splits triangles that touch more than kMaxRecordTiles
+// tiles into sub-records.
 #include <float.h>
 
 #include <algorithm>
