@@ -1,4 +1,4 @@
-"""The oracle timed on the host's cores — TEST / BASELINE INFRASTRUCTURE ONLY.
+"""The oracle timed on the host's cores — TEST AND CPU-BASELINE INFRASTRUCTURE ONLY.
 
 Used by bench.py's ``cpu_baseline`` leg and its ``--impl reference`` arm, never by the
 product.  The reference renders on one thread (main.cpp:87-155), so its throughput on a
